@@ -1,0 +1,314 @@
+"""Benchmark: CCD++ rank-one updates/s on the 480,189 x 17,770 / 99.07M-train-nnz
+synthetic (Netflix-shaped), k=64, lambda=0.05, 1 inner iteration.
+
+One step = one outer iteration = 64 rank-one updates (each: add-back, one CSC
+and one CSR sweep, subtract) + the fused test RMSE, with the matrix resident
+in HBM.  The residual copies (1.6 GB at FP32) are far larger than L2, so no
+L2 flush is needed between steps.
+
+Printed as one JSON line (rank 0):
+  value  -- updates/s, device-resident, CUDA events on the engine stream
+  e2e    -- updates/s through cdmf_cuda_train (the reference's engine call)
+            from page-locked host buffers: upload of R, 20 outer iterations
+            with a per-iteration RMSE read-back, download of W and H
+  roofline -- the sweep kernel: compulsory bytes per launch / mean launch time
+  cpu_baseline -- the oracle CPU port of the reference engine on the host cores
+
+--impl reference: the reference's CPU engine (oracle port; the reference
+sources are not on the GPU host) on the same workload, one bounded sample per
+step, all host threads.
+
+Multi-GPU: `torchrun --nproc-per-node N bench.py --gpus N` runs one
+independent replica per GPU (weak scaling, no collective in the data path);
+rank 0 prints updates/s summed over ranks, timed as the max over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "CCD++ rank-one updates/s & HBM GB/s at matched test RMSE, mixed vs FP32"
+UNIT = "rank-one updates/s"
+WORKLOAD = "netflix_shape"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, ws, rank):
+        self.ws, self.rank = ws, rank
+        self.pg = None
+        if ws > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=rank, world_size=ws)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per sweep launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "sweep_traffic.json")
+    if os.path.exists(path):
+        try:
+            return json.load(open(path))
+        except Exception:
+            return None
+    return None
+
+
+def cpu_sample(R, run, W0, threads, budget_s):
+    """Oracle port of cdmf_ref on the host cores: features of one steady-state
+    outer iteration (add-back on) until budget_s is spent.  Returns
+    (updates/s, features timed, seconds)."""
+    from oracle import oracle
+    k = run["k"]
+    done, spent = 0, 0.0
+    rc, rr = R.csc_val.copy(), R.csr_val.copy()
+    H = np.zeros((1, R.n), np.float32)
+    while done < k and (spent < budget_s or done == 0):
+        W = np.ascontiguousarray(W0[done:done + 1])
+        t0 = time.perf_counter()
+        oracle.outer_iteration(R, W, H, rc, rr, 1, run["lambda_"], run["maxinneriter"], 2, threads=threads)
+        spent += time.perf_counter() - t0
+        done += 1
+    return done / spent, done, spent
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
+    ap.add_argument("--residual", default="f32", choices=["f32", "bf16", "f16"])
+    ap.add_argument("--k", type=int, default=64)
+    ap.add_argument("--e2e-outer", type=int, default=20)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    args.warmup = max(3, args.warmup)
+
+    from cdmf_gb300 import synth
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from oracle import oracle  # noqa: F401
+        R, run = synth.config(WORKLOAD, threads=threads)
+        run["k"] = args.k
+        W0 = synth.initial_w(run["k"], R.m, seed=0)
+        for _ in range(args.warmup):
+            cpu_sample(R, run, W0, threads, 0.0)
+        vals, feats, secs = [], 0, 0.0
+        for _ in range(args.steps):
+            v, f, s = cpu_sample(R, run, W0, threads, max(1.0, args.cpu_budget / max(1, args.steps)))
+            vals.append(v)
+            feats += f
+            secs += s
+        value = feats / secs
+        line = {
+            "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded, Netflix-shaped)",
+            "config": {"workload": f"{WORKLOAD} {R.m}x{R.n} nnz={R.nnz} k={run['k']} lambda={run['lambda_']} "
+                                   f"T={run['maxinneriter']}", "sample": "features of one outer iteration"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{feats} rank-one updates of a steady-state outer iteration on the full "
+                                       f"matrix, {secs:.1f} s, OpenMP over {threads} threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return
+
+    from cdmf_gb300 import engine, _lib
+    dist = Dist(ws, rank)
+    device = local
+    R, run = synth.config(WORKLOAD, threads=threads)
+    run["k"] = args.k
+    k, lam, T = run["k"], run["lambda_"], run["maxinneriter"]
+    W0 = synth.initial_w(k, R.m, seed=rank)
+
+    e = engine.Engine(R, k, lam, maxiter=max(args.steps, args.e2e_outer), maxinneriter=T, residual=args.residual,
+                      device=device)
+    e.set_factors(W0)
+    e.run(args.warmup)
+    # timed: device-resident
+    dist.barrier()
+    with ClockSampler(device) as clk:
+        rm = e.run(args.steps)
+        st = e.stats()
+    t_ms = dist.max(st["train_ms"])
+    dist.barrier()
+    updates = st["updates"]
+    value = ws * updates / (t_ms / 1e3)
+    launches = st["launches"]
+    # roofline pass: per-launch events around the sweeps
+    e.set_profiling(True)
+    e.run(2)
+    sp = e.stats()
+    e.set_profiling(False)
+    n_sweeps = sp["sweep_csc_launches"] + sp["sweep_csr_launches"]
+    sweep_ms = sp["sweep_csc_ms"] + sp["sweep_csr_ms"]
+    bytes_launch = sp["bytes_per_update"] / (2 * T)
+    mean_launch_s = sweep_ms / 1e3 / n_sweeps
+    peak, peak_kind = measured_peak()
+    achieved = bytes_launch / mean_launch_s / 1e9
+    tr = profiled_traffic()
+    traffic = None
+    if tr and tr.get("workload") == WORKLOAD and tr.get("residual") == args.residual:
+        traffic = tr.get("dram_bytes_per_launch")
+    test_rmse = float(rm[-1]) if rm is not None else None
+    e.close()
+
+    # e2e through the one-shot engine call from page-locked host memory
+    arrays = {}
+    owners = []
+    for name in ("csr_ptr", "csr_idx", "csr_val", "csc_ptr", "csc_idx", "csc_val", "te_row", "te_col", "te_val"):
+        src = getattr(R, name)
+        a, o = _lib.pinned_empty(src.shape, src.dtype)
+        a[...] = src
+        arrays[name] = a
+        owners.append(o)
+    from cdmf_gb300.formats import RatingMatrix
+    Rp = RatingMatrix(R.m, R.n, **arrays)
+    Wp, ow = _lib.pinned_empty(W0.shape, np.float32)
+    owners.append(ow)
+    h2d = sum(getattr(Rp, f).nbytes for f in arrays) + W0.nbytes
+    d2h = W0.nbytes + 4 * k * R.n + 8 * args.e2e_outer
+    Wp[...] = W0
+    engine.train(Rp, Wp, k, lam, 1, T, residual=args.residual, device=device)  # warm the context
+    dist.barrier()
+    t0 = time.perf_counter()
+    Wp[...] = W0
+    _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, residual=args.residual, device=device)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = ws * k * args.e2e_outer / e2e_s
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        v, f, s = cpu_sample(R, run, W0, threads, args.cpu_budget)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{f} rank-one updates of a steady-state outer iteration (k={k}) on the full matrix, "
+                         f"{s:.1f} s, oracle port of src/cdmf_ref.cpp, OpenMP over {threads} threads"}
+    dist.close()
+    if rank != 0:
+        return
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.residual == "f32" else f"{args.residual} residual, f32 factors and accumulation",
+        "data": "synthetic (seeded, Netflix-shaped; the data set itself is not available)",
+        "config": {"workload": f"{WORKLOAD} {R.m}x{R.n} train_nnz={R.nnz} test_nnz={R.nnz_test} k={k} "
+                               f"lambda={lam} T={T}",
+                   "residual": args.residual, "step": "one outer iteration (k rank-one updates + test RMSE)",
+                   "l2": "no flush: the residual copies streamed every feature exceed L2",
+                   "parallelism": f"replicas x{ws}"},
+        "outer_per_s": 1e3 * args.steps / t_ms,
+        "hbm_gbs_sweeps": achieved,
+        "test_rmse": test_rmse,
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "sweep_kernel (CSC h-sweep + CSR w-sweep)",
+                     "bytes_per_launch": bytes_launch, "mean_launch_ms": mean_launch_s * 1e3},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "step": f"one cdmf_cuda_train call: upload, {args.e2e_outer} outer iterations, download",
+                "seconds": e2e_s, "test_rmse": float(e2e_rm[-1])},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

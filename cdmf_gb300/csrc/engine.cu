@@ -1,0 +1,698 @@
+// CCD++ engine on one GB300: the C ABI of include/cdmf_cuda.h.
+//
+// Schedule of one outer iteration (src/cdmf_ref.cpp:69-137), per feature t:
+//   inner 1:  CSC sweep  -> H[t]   (+ pending subtract of feature t-1, + add-back of t)
+//             CSR sweep  -> W[t]   (+ pending subtract of feature t-1, + add-back of t)
+//   inner 2..T: the same two sweeps without residual writes
+// The subtract of feature t (src/cdmf_ref.cpp:120-121) is carried into the
+// first sweeps of feature t+1 (or of the next outer iteration), so every
+// residual element is read and written once per feature per copy.  The
+// operations on an element happen in the reference's order (subtract t, then
+// add back t+1), so the arithmetic is unchanged; only the number of passes
+// over HBM drops from 6 to 2.
+//
+// The reference reads W[t], H[t] into u, v and writes them back after the
+// inner loop (src/cdmf_ref.cpp:80-83,115-118).  Here the CSC sweep overwrites
+// H[t] in place and keeps the old H[t] in `hsave` (the CSR add-back needs it);
+// the CSR sweep overwrites W[t] in place (each row reads only its own old
+// w_i before writing it).
+#include "../../include/cdmf_cuda.h"
+#include "sweep_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace cdmf;
+
+namespace {
+
+struct Bins {
+    std::vector<XTask> x;
+    std::vector<uint32_t> c, w, t;
+    uint32_t nslots = 0, nxl = 0;
+    int64_t count[4] = {0, 0, 0, 0}, nnz[4] = {0, 0, 0, 0};
+};
+
+struct DevBins {
+    XTask* x = nullptr;
+    uint32_t *c = nullptr, *w = nullptr, *t = nullptr;
+    float2* part = nullptr;
+    uint32_t* xcount = nullptr;
+    uint32_t nx = 0, nc = 0, nw = 0, nt = 0, nwb = 0, ntb = 0;
+    Bins host;
+};
+
+// Bin thresholds (line length in nonzeros).
+struct BinCfg {
+    uint32_t thread_max = 12;    // <= : one thread per line
+    uint32_t warp_max = 2048;    // <= : one warp per line
+    uint32_t cta_max = 16384;    // <= : one CTA per line; above: split
+    uint32_t chunk = 8192;       // nonzeros per chunk of a split line
+};
+
+Bins plan_bins(const uint32_t* ptr, int64_t lines, bool sequential, const BinCfg& cfg) {
+    Bins B;
+    for (int64_t j = 0; j < lines; ++j) {
+        const uint32_t len = ptr[j + 1] - ptr[j];
+        int bin;
+        if (sequential || len <= cfg.thread_max) bin = 0;
+        else if (len <= cfg.warp_max) bin = 1;
+        else if (len <= cfg.cta_max) bin = 2;
+        else bin = 3;
+        B.count[bin]++;
+        B.nnz[bin] += len;
+        switch (bin) {
+            case 0: B.t.push_back((uint32_t)j); break;
+            case 1: B.w.push_back((uint32_t)j); break;
+            case 2: B.c.push_back((uint32_t)j); break;
+            default: {
+                const uint32_t nch = (len + cfg.chunk - 1) / cfg.chunk;
+                const uint32_t first = B.nslots;
+                for (uint32_t q = 0; q < nch; ++q) {
+                    XTask T;
+                    T.line = (uint32_t)j;
+                    T.beg = ptr[j] + q * cfg.chunk;
+                    T.end = std::min<uint32_t>(ptr[j + 1], T.beg + cfg.chunk);
+                    T.slot = first + q;
+                    T.xl = B.nxl;
+                    T.first_slot = first;
+                    T.nchunks = nch;
+                    T.pad = 0;
+                    B.x.push_back(T);
+                }
+                B.nslots += nch;
+                B.nxl++;
+            }
+        }
+    }
+    // longest lines first inside the CTA bin so the tail of the launch is short
+    std::stable_sort(B.c.begin(), B.c.end(), [&](uint32_t a, uint32_t b) {
+        return (ptr[a + 1] - ptr[a]) > (ptr[b + 1] - ptr[b]);
+    });
+    return B;
+}
+
+const char* kErrStr[] = {"ok",          "invalid argument or sparse structure", "allocation failed",
+                         "CUDA error",  "no CUDA device",                        "empty test set",
+                         "numeric check failed", "unsupported option",           "size beyond limit"};
+
+}  // namespace
+
+struct cdmf_handle {
+    cdmf_opts o{};
+    int64_t m = 0, n = 0, nnz = 0, nt = 0;
+    int rt = 0;                      // residual type 0/1/2
+    size_t rbytes = 4;
+    cudaStream_t s = nullptr;
+    // device arrays
+    uint32_t *csr_ptr = nullptr, *csr_idx = nullptr, *csc_ptr = nullptr, *csc_idx = nullptr;
+    float *csr_val = nullptr, *csc_val = nullptr;  // pristine ratings
+    void *res_csr = nullptr, *res_csc = nullptr;   // residual copies
+    float *W = nullptr, *H = nullptr, *hsave = nullptr;
+    uint32_t *te_row = nullptr, *te_col = nullptr;
+    float* te_val = nullptr;
+    double *rmse_part = nullptr, *rmse_out = nullptr;
+    uint32_t* rmse_count = nullptr;
+    int rmse_grid = 0;
+    DevBins csr, csc;
+    // state
+    int next_oiter = 1;
+    int pending = -1;                // feature whose subtract is still owed, -1 = none
+    // timing
+    bool profiling = false;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    struct Mark { int kind; cudaEvent_t a, b; };
+    std::vector<Mark> marks;
+    std::vector<cudaEvent_t> pool;
+    size_t pool_used = 0;
+    cdmf_stats st{};
+    std::string err;
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+int fail(cdmf_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+#define CU(h, call)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(h, CDMF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int dalloc(cdmf_handle* h, T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(h, CDMF_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    h->allocs.push_back((void*)*p);
+    return CDMF_OK;
+}
+
+int check_compressed(const uint32_t* ptr, const uint32_t* idx, int64_t lines, int64_t cross, int64_t nnz) {
+    if (!ptr || (nnz > 0 && !idx)) return CDMF_ERR_INVALID;
+    if (ptr[0] != 0 || (int64_t)ptr[lines] != nnz) return CDMF_ERR_INVALID;
+    for (int64_t j = 0; j < lines; ++j)
+        if (ptr[j] > ptr[j + 1]) return CDMF_ERR_INVALID;
+    for (int64_t q = 0; q < nnz; ++q)
+        if ((int64_t)idx[q] >= cross) return CDMF_ERR_INVALID;
+    return CDMF_OK;
+}
+
+int upload_bins(cdmf_handle* h, DevBins& D, Bins&& B) {
+    D.nx = (uint32_t)B.x.size();
+    D.nc = (uint32_t)B.c.size();
+    D.nw = (uint32_t)B.w.size();
+    D.nt = (uint32_t)B.t.size();
+    D.nwb = (D.nw + kWarps - 1) / kWarps;
+    D.ntb = (D.nt + kBlock - 1) / kBlock;
+    int r;
+    if ((r = dalloc(h, &D.x, B.x.size())) || (r = dalloc(h, &D.c, B.c.size())) || (r = dalloc(h, &D.w, B.w.size())) ||
+        (r = dalloc(h, &D.t, B.t.size())) || (r = dalloc(h, &D.part, B.nslots)) || (r = dalloc(h, &D.xcount, B.nxl)))
+        return r;
+    if (D.nx) CU(h, cudaMemcpyAsync(D.x, B.x.data(), sizeof(XTask) * D.nx, cudaMemcpyHostToDevice, h->s));
+    if (D.nc) CU(h, cudaMemcpyAsync(D.c, B.c.data(), 4 * D.nc, cudaMemcpyHostToDevice, h->s));
+    if (D.nw) CU(h, cudaMemcpyAsync(D.w, B.w.data(), 4 * D.nw, cudaMemcpyHostToDevice, h->s));
+    if (D.nt) CU(h, cudaMemcpyAsync(D.t, B.t.data(), 4 * D.nt, cudaMemcpyHostToDevice, h->s));
+    CU(h, cudaMemsetAsync(D.xcount, 0, 4 * std::max<uint32_t>(1, B.nxl), h->s));
+    CU(h, cudaStreamSynchronize(h->s));  // host vectors are released below
+    D.host = std::move(B);
+    D.host.x.clear(); D.host.x.shrink_to_fit();
+    D.host.c.clear(); D.host.c.shrink_to_fit();
+    D.host.w.clear(); D.host.w.shrink_to_fit();
+    D.host.t.clear(); D.host.t.shrink_to_fit();
+    return CDMF_OK;
+}
+
+cudaEvent_t pool_event(cdmf_handle* h) {
+    if (h->pool_used == h->pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        h->pool.push_back(e);
+    }
+    return h->pool[h->pool_used++];
+}
+
+enum { K_CSC = 0, K_CSR = 1, K_RMSE = 2, K_REFRESH = 3 };
+
+struct Timed {
+    cdmf_handle* h;
+    int kind;
+    cudaEvent_t b = nullptr;
+    Timed(cdmf_handle* h_, int kind_) : h(h_), kind(kind_) {
+        if (h->profiling) {
+            cudaEvent_t a = pool_event(h);
+            b = pool_event(h);
+            if (a && b) {
+                cudaEventRecord(a, h->s);
+                h->marks.push_back({kind, a, b});
+            } else {
+                b = nullptr;
+            }
+        }
+    }
+    ~Timed() {
+        if (b) cudaEventRecord(b, h->s);
+    }
+};
+
+template <int RT>
+void launch_sweep_rt(const SweepArgs& A, bool sub, bool add, unsigned grid, cudaStream_t s) {
+    if (sub && add) sweep_kernel<RT, true, true><<<grid, kBlock, 0, s>>>(A);
+    else if (sub) sweep_kernel<RT, true, false><<<grid, kBlock, 0, s>>>(A);
+    else if (add) sweep_kernel<RT, false, true><<<grid, kBlock, 0, s>>>(A);
+    else sweep_kernel<RT, false, false><<<grid, kBlock, 0, s>>>(A);
+}
+
+int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const uint32_t* ptr, const uint32_t* idx, void* res,
+                 const float* a, const float* b, const float* c, const float* d, const float* y, float* out,
+                 float* save) {
+    SweepArgs A;
+    A.ptr = ptr;
+    A.idx = idx;
+    A.res = res;
+    A.a = a;
+    A.b = b;
+    A.c = c;
+    A.d = d;
+    A.y = y;
+    A.out = out;
+    A.save = save;
+    A.lambda = h->o.lambda;
+    A.xt = D.x;
+    A.cl = D.c;
+    A.wl = D.w;
+    A.tl = D.t;
+    A.nx = D.nx;
+    A.nc = D.nc;
+    A.nw = D.nw;
+    A.nt = D.nt;
+    A.nwb = D.nwb;
+    A.part = D.part;
+    A.xcount = D.xcount;
+    const unsigned grid = D.nx + D.nc + D.nwb + D.ntb;
+    if (grid == 0) return CDMF_OK;
+    {
+        Timed tm(h, kind);
+        switch (h->rt) {
+            case 0: launch_sweep_rt<0>(A, a != nullptr, c != nullptr, grid, h->s); break;
+            case 1: launch_sweep_rt<1>(A, a != nullptr, c != nullptr, grid, h->s); break;
+            default: launch_sweep_rt<2>(A, a != nullptr, c != nullptr, grid, h->s); break;
+        }
+    }
+    CU(h, cudaGetLastError());
+    h->st.launches++;
+    if (kind == K_CSC) h->st.sweep_csc_launches++;
+    else h->st.sweep_csr_launches++;
+    return CDMF_OK;
+}
+
+// One feature t of outer iteration `oiter`.
+int feature_step(cdmf_handle* h, uint32_t t, int oiter) {
+    const int64_t m = h->m, n = h->n;
+    float* Wt = h->W + (size_t)t * m;
+    float* Ht = h->H + (size_t)t * n;
+    const int tp = h->pending;
+    const float* Wp = tp >= 0 ? h->W + (size_t)tp * m : nullptr;
+    const float* Hp = tp >= 0 ? h->H + (size_t)tp * n : nullptr;
+    const bool add = oiter > 1;
+    int r;
+    for (int it = 1; it <= h->o.maxinneriter; ++it) {
+        const bool first = it == 1;
+        // h_t over CSC: cross vectors are rows (length m)
+        r = launch_sweep(h, K_CSC, h->csc, h->csc_ptr, h->csc_idx, h->res_csc, first ? Wp : nullptr,
+                         first ? Hp : nullptr, first && add ? Wt : nullptr, first && add ? Ht : nullptr, Wt, Ht,
+                         first ? h->hsave : nullptr);
+        if (r) return r;
+        // w_t over CSR: cross vectors are columns (length n).  H[tp] was
+        // overwritten above when tp == t (k == 1); hsave holds its old value.
+        const float* Hp_csr = (tp == (int)t) ? h->hsave : Hp;
+        r = launch_sweep(h, K_CSR, h->csr, h->csr_ptr, h->csr_idx, h->res_csr, first ? Hp_csr : nullptr,
+                         first ? Wp : nullptr, first && add ? h->hsave : nullptr, first && add ? Wt : nullptr, Ht, Wt,
+                         nullptr);
+        if (r) return r;
+    }
+    if (h->o.maxinneriter > 0) h->pending = (int)t;
+    return CDMF_OK;
+}
+
+int launch_rmse(cdmf_handle* h, double* dst) {
+    Timed tm(h, K_RMSE);
+    rmse_kernel<<<h->rmse_grid, kBlock, 0, h->s>>>(h->te_row, h->te_col, h->te_val, h->nt, h->W, h->H, h->m, h->n,
+                                                  h->o.k, h->rmse_part, h->rmse_count, dst);
+    CU(h, cudaGetLastError());
+    h->st.launches++;
+    h->st.rmse_launches++;
+    return CDMF_OK;
+}
+
+int flush_pending(cdmf_handle* h) {
+    if (h->pending < 0) return CDMF_OK;
+    const int tp = h->pending;
+    const float* Wp = h->W + (size_t)tp * h->m;
+    const float* Hp = h->H + (size_t)tp * h->n;
+    const unsigned gc = (unsigned)std::min<int64_t>(4096, (h->n + kWarps - 1) / kWarps + 1);
+    const unsigned gr = (unsigned)std::min<int64_t>(4096, (h->m + kWarps - 1) / kWarps + 1);
+    switch (h->rt) {
+        case 0:
+            flush_kernel<0><<<gc, kBlock, 0, h->s>>>(h->csc_ptr, h->csc_idx, h->res_csc, Wp, Hp, (uint32_t)h->n);
+            flush_kernel<0><<<gr, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->res_csr, Hp, Wp, (uint32_t)h->m);
+            break;
+        case 1:
+            flush_kernel<1><<<gc, kBlock, 0, h->s>>>(h->csc_ptr, h->csc_idx, h->res_csc, Wp, Hp, (uint32_t)h->n);
+            flush_kernel<1><<<gr, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->res_csr, Hp, Wp, (uint32_t)h->m);
+            break;
+        default:
+            flush_kernel<2><<<gc, kBlock, 0, h->s>>>(h->csc_ptr, h->csc_idx, h->res_csc, Wp, Hp, (uint32_t)h->n);
+            flush_kernel<2><<<gr, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->res_csr, Hp, Wp, (uint32_t)h->m);
+            break;
+    }
+    CU(h, cudaGetLastError());
+    h->pending = -1;
+    return CDMF_OK;
+}
+
+__global__ void f32_to_res_kernel(const float* __restrict__ src, void* __restrict__ dst, int64_t count, int rt) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
+        if (rt == 1) ((__nv_bfloat16*)dst)[q] = __float2bfloat16_rn(src[q]);
+        else ((__half*)dst)[q] = __float2half_rn(src[q]);
+    }
+}
+__global__ void res_to_f32_kernel(const void* __restrict__ src, float* __restrict__ dst, int64_t count, int rt) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
+        if (rt == 1) dst[q] = __bfloat162float(((const __nv_bfloat16*)src)[q]);
+        else dst[q] = __half2float(((const __half*)src)[q]);
+    }
+}
+
+// dst residual := src ratings (device, float)
+int reset_residual(cdmf_handle* h, void* dst, const float* src) {
+    if (h->nnz == 0) return CDMF_OK;
+    if (h->rt == 0) {
+        CU(h, cudaMemcpyAsync(dst, src, sizeof(float) * h->nnz, cudaMemcpyDeviceToDevice, h->s));
+    } else {
+        f32_to_res_kernel<<<1216, 256, 0, h->s>>>(src, dst, h->nnz, h->rt);
+        CU(h, cudaGetLastError());
+    }
+    return CDMF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void cdmf_opts_default(cdmf_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->k = 10;                 // src/pmf.h:17-18 defaults
+    o->lambda = 0.1f;
+    o->maxiter = 5;
+    o->maxinneriter = 5;
+    o->version = 1;
+    o->residual = CDMF_RES_F32;
+    o->reduce = CDMF_REDUCE_TREE;
+    o->rmse_each_outer = 1;
+    o->use_graph = 0;
+    o->threads_per_block = 0;
+    o->device = 0;
+    o->verbose = 0;
+}
+
+const char* cdmf_cuda_strerror(int status) {
+    if (status > 0 || status < -8) return "unknown status";
+    return kErrStr[-status];
+}
+
+int cdmf_cuda_version(void) { return 100; }
+
+void* cdmf_cuda_host_alloc(uint64_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void cdmf_cuda_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+const char* cdmf_cuda_last_error(const cdmf_handle* h) { return h ? h->err.c_str() : ""; }
+
+void cdmf_cuda_destroy(cdmf_handle* h) {
+    if (!h) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaSetDevice(h->o.device);
+    if (h->s) cudaStreamSynchronize(h->s);
+    for (void* p : h->allocs) cudaFree(p);
+    for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
+    if (h->ev_start) cudaEventDestroy(h->ev_start);
+    if (h->ev_stop) cudaEventDestroy(h->ev_stop);
+    if (h->s) cudaStreamDestroy(h->s);
+    cudaSetDevice(dev);
+    delete h;
+}
+
+int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** out) {
+    if (!out) return CDMF_ERR_INVALID;
+    *out = nullptr;
+    if (!p || !o) return CDMF_ERR_INVALID;
+    if (p->m < 0 || p->n < 0 || p->nnz < 0 || p->nnz_test < 0 || o->k == 0 || o->maxinneriter < 0 ||
+        o->maxiter < 0 || !(o->lambda >= 0.0f))
+        return CDMF_ERR_INVALID;
+    if (o->residual < 0 || o->residual > 2 || o->reduce < 0 || o->reduce > 1 || o->version < 1 || o->version > 3)
+        return CDMF_ERR_INVALID;
+    if (p->nnz > (int64_t)UINT32_MAX || p->m >= (int64_t)UINT32_MAX || p->n >= (int64_t)UINT32_MAX ||
+        p->nnz_test > (int64_t)INT32_MAX * 64)
+        return CDMF_ERR_TOO_LARGE;
+    int r;
+    if ((r = check_compressed(p->csr_row_ptr, p->csr_col_idx, p->m, p->n, p->nnz))) return r;
+    if ((r = check_compressed(p->csc_col_ptr, p->csc_row_idx, p->n, p->m, p->nnz))) return r;
+    if (p->nnz > 0 && (!p->csr_val || !p->csc_val)) return CDMF_ERR_INVALID;
+    if (p->nnz_test > 0) {
+        if (!p->test_row || !p->test_col || !p->test_val) return CDMF_ERR_INVALID;
+        for (int64_t e = 0; e < p->nnz_test; ++e)
+            if ((int64_t)p->test_row[e] >= p->m || (int64_t)p->test_col[e] >= p->n) return CDMF_ERR_INVALID;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CDMF_ERR_NO_DEVICE;
+    if (o->device < 0 || o->device >= ndev) return CDMF_ERR_NO_DEVICE;
+
+    cdmf_handle* h = new cdmf_handle();
+    h->o = *o;
+    h->m = p->m;
+    h->n = p->n;
+    h->nnz = p->nnz;
+    h->nt = p->nnz_test;
+    h->rt = o->residual;
+    h->rbytes = o->residual == CDMF_RES_F32 ? 4 : 2;
+    auto bail = [&](int code) { cdmf_cuda_destroy(h); return code; };
+    if (cudaSetDevice(o->device) != cudaSuccess) return bail(CDMF_ERR_NO_DEVICE);
+    if (cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    if (cudaEventCreate(&h->ev_start) != cudaSuccess || cudaEventCreate(&h->ev_stop) != cudaSuccess)
+        return bail(CDMF_ERR_CUDA);
+    const int64_t m = p->m, n = p->n, N = p->nnz, k = o->k;
+    if ((r = dalloc(h, &h->csr_ptr, m + 1)) || (r = dalloc(h, &h->csr_idx, N)) || (r = dalloc(h, &h->csc_ptr, n + 1)) ||
+        (r = dalloc(h, &h->csc_idx, N)) || (r = dalloc(h, &h->csr_val, N)) || (r = dalloc(h, &h->csc_val, N)) ||
+        (r = dalloc(h, (char**)&h->res_csr, N * h->rbytes)) || (r = dalloc(h, (char**)&h->res_csc, N * h->rbytes)) ||
+        (r = dalloc(h, &h->W, k * m)) || (r = dalloc(h, &h->H, k * n)) || (r = dalloc(h, &h->hsave, n)) ||
+        (r = dalloc(h, &h->te_row, h->nt)) || (r = dalloc(h, &h->te_col, h->nt)) || (r = dalloc(h, &h->te_val, h->nt)))
+        return bail(r);
+    h->rmse_grid = (int)std::max<int64_t>(1, std::min<int64_t>(4 * 152, (h->nt + kBlock - 1) / kBlock));
+    if ((r = dalloc(h, &h->rmse_part, h->rmse_grid)) || (r = dalloc(h, &h->rmse_out, 1 + std::max(0, o->maxiter))) ||
+        (r = dalloc(h, &h->rmse_count, 1)))
+        return bail(r);
+    auto up = [&](void* dst, const void* src, size_t bytes) -> int {
+        if (bytes == 0) return CDMF_OK;
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->s);
+        if (e != cudaSuccess) return fail(h, CDMF_ERR_CUDA, cudaGetErrorString(e));
+        return CDMF_OK;
+    };
+    if ((r = up(h->csr_ptr, p->csr_row_ptr, 4 * (m + 1))) || (r = up(h->csr_idx, p->csr_col_idx, 4 * N)) ||
+        (r = up(h->csc_ptr, p->csc_col_ptr, 4 * (n + 1))) || (r = up(h->csc_idx, p->csc_row_idx, 4 * N)) ||
+        (r = up(h->csr_val, p->csr_val, 4 * N)) || (r = up(h->csc_val, p->csc_val, 4 * N)) ||
+        (r = up(h->te_row, p->test_row, 4 * h->nt)) || (r = up(h->te_col, p->test_col, 4 * h->nt)) ||
+        (r = up(h->te_val, p->test_val, 4 * h->nt)))
+        return bail(r);
+    if (cudaMemsetAsync(h->rmse_count, 0, 4, h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    const bool seq = o->reduce == CDMF_REDUCE_SEQUENTIAL;
+    BinCfg cfg;
+    if ((r = upload_bins(h, h->csr, plan_bins(p->csr_row_ptr, m, seq, cfg))) ||
+        (r = upload_bins(h, h->csc, plan_bins(p->csc_col_ptr, n, seq, cfg))))
+        return bail(r);
+    // fresh state: W := 0 until set, H := 0, residual := ratings
+    if (cudaMemsetAsync(h->W, 0, sizeof(float) * k * m, h->s) != cudaSuccess ||
+        cudaMemsetAsync(h->H, 0, sizeof(float) * k * n, h->s) != cudaSuccess)
+        return bail(CDMF_ERR_CUDA);
+    if ((r = reset_residual(h, h->res_csr, h->csr_val)) || (r = reset_residual(h, h->res_csc, h->csc_val)))
+        return bail(r);
+    if (cudaStreamSynchronize(h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    const double T = std::max(1, o->maxinneriter);
+    const double br = (double)h->rbytes;
+    h->st.bytes_per_update = T * 2.0 * N * (4.0 + br) + 2.0 * N * br + T * 4.0 * (m + n + 2) + 8.0 * (m + n);
+    *out = h;
+    return CDMF_OK;
+}
+
+int cdmf_cuda_set_factors(cdmf_handle* h, const float* W0, const float* H0) {
+    if (!h) return CDMF_ERR_INVALID;
+    CU(h, cudaSetDevice(h->o.device));
+    const size_t wb = sizeof(float) * h->o.k * h->m, hb = sizeof(float) * h->o.k * h->n;
+    if (W0) CU(h, cudaMemcpyAsync(h->W, W0, wb, cudaMemcpyHostToDevice, h->s));
+    else CU(h, cudaMemsetAsync(h->W, 0, wb, h->s));
+    if (H0) CU(h, cudaMemcpyAsync(h->H, H0, hb, cudaMemcpyHostToDevice, h->s));
+    else CU(h, cudaMemsetAsync(h->H, 0, hb, h->s));
+    int r;
+    if ((r = reset_residual(h, h->res_csr, h->csr_val)) || (r = reset_residual(h, h->res_csc, h->csc_val))) return r;
+    h->pending = -1;
+    h->next_oiter = 1;
+    CU(h, cudaStreamSynchronize(h->s));
+    return CDMF_OK;
+}
+
+int cdmf_cuda_run(cdmf_handle* h, int n_outer, double* rmse_out) {
+    if (!h || n_outer < 0) return CDMF_ERR_INVALID;
+    if (rmse_out && h->o.rmse_each_outer && h->nt == 0) return fail(h, CDMF_ERR_EMPTY_TEST, "empty test set");
+    CU(h, cudaSetDevice(h->o.device));
+    h->st.train_ms = 0;
+    h->st.sweep_csc_ms = h->st.sweep_csr_ms = h->st.rmse_ms = h->st.refresh_ms = 0;
+    h->st.launches = h->st.sweep_csc_launches = h->st.sweep_csr_launches = 0;
+    h->st.rmse_launches = h->st.refresh_launches = 0;
+    h->st.updates = 0;
+    h->marks.clear();
+    h->pool_used = 0;
+    std::vector<double> rm(std::max(1, n_outer), 0.0);
+    // rmse values land in a device ring of maxiter+1 slots, copied back per chunk
+    const int slots = 1 + std::max(0, h->o.maxiter);
+    CU(h, cudaEventRecord(h->ev_start, h->s));
+    int done = 0;
+    while (done < n_outer) {
+        const int chunk = std::min(n_outer - done, slots);
+        for (int q = 0; q < chunk; ++q) {
+            const int oiter = h->next_oiter;
+            for (uint32_t t = 0; t < h->o.k; ++t) {
+                int r = feature_step(h, t, oiter);
+                if (r) return r;
+            }
+            h->st.updates += h->o.k;
+            if (h->o.rmse_each_outer && h->nt > 0) {
+                int r = launch_rmse(h, h->rmse_out + q);
+                if (r) return r;
+            }
+            h->next_oiter++;
+        }
+        if (rmse_out && h->o.rmse_each_outer && h->nt > 0) {
+            CU(h, cudaMemcpyAsync(rm.data() + done, h->rmse_out, sizeof(double) * chunk, cudaMemcpyDeviceToHost, h->s));
+            CU(h, cudaStreamSynchronize(h->s));
+        }
+        done += chunk;
+    }
+    CU(h, cudaEventRecord(h->ev_stop, h->s));
+    CU(h, cudaEventSynchronize(h->ev_stop));
+    float ms = 0;
+    CU(h, cudaEventElapsedTime(&ms, h->ev_start, h->ev_stop));
+    h->st.train_ms = ms;
+    for (const auto& mk : h->marks) {
+        float t = 0;
+        if (cudaEventElapsedTime(&t, mk.a, mk.b) != cudaSuccess) continue;
+        if (mk.kind == K_CSC) h->st.sweep_csc_ms += t;
+        else if (mk.kind == K_CSR) h->st.sweep_csr_ms += t;
+        else if (mk.kind == K_RMSE) h->st.rmse_ms += t;
+        else h->st.refresh_ms += t;
+    }
+    if (rmse_out) for (int q = 0; q < n_outer; ++q) rmse_out[q] = rm[q];
+    return CDMF_OK;
+}
+
+int cdmf_cuda_get_factors(cdmf_handle* h, float* W, float* H) {
+    if (!h) return CDMF_ERR_INVALID;
+    CU(h, cudaSetDevice(h->o.device));
+    if (W) CU(h, cudaMemcpyAsync(W, h->W, sizeof(float) * h->o.k * h->m, cudaMemcpyDeviceToHost, h->s));
+    if (H) CU(h, cudaMemcpyAsync(H, h->H, sizeof(float) * h->o.k * h->n, cudaMemcpyDeviceToHost, h->s));
+    CU(h, cudaStreamSynchronize(h->s));
+    return CDMF_OK;
+}
+
+int cdmf_cuda_rmse(cdmf_handle* h, double* rmse) {
+    if (!h || !rmse) return CDMF_ERR_INVALID;
+    if (h->nt == 0) return fail(h, CDMF_ERR_EMPTY_TEST, "empty test set");
+    CU(h, cudaSetDevice(h->o.device));
+    int r = launch_rmse(h, h->rmse_out);
+    if (r) return r;
+    CU(h, cudaMemcpyAsync(rmse, h->rmse_out, sizeof(double), cudaMemcpyDeviceToHost, h->s));
+    CU(h, cudaStreamSynchronize(h->s));
+    return CDMF_OK;
+}
+
+int cdmf_cuda_get_state(cdmf_handle* h, float* W, float* H, float* res_csc, float* res_csr, int* next_oiter) {
+    if (!h) return CDMF_ERR_INVALID;
+    CU(h, cudaSetDevice(h->o.device));
+    int r = flush_pending(h);
+    if (r) return r;
+    if ((r = cdmf_cuda_get_factors(h, W, H))) return r;
+    auto down = [&](float* dst, void* src) -> int {
+        if (!dst || h->nnz == 0) return CDMF_OK;
+        if (h->rt == 0) {
+            CU(h, cudaMemcpyAsync(dst, src, sizeof(float) * h->nnz, cudaMemcpyDeviceToHost, h->s));
+        } else {
+            float* tmp = nullptr;
+            CU(h, cudaMallocAsync((void**)&tmp, sizeof(float) * h->nnz, h->s));
+            res_to_f32_kernel<<<1216, 256, 0, h->s>>>(src, tmp, h->nnz, h->rt);
+            CU(h, cudaGetLastError());
+            CU(h, cudaMemcpyAsync(dst, tmp, sizeof(float) * h->nnz, cudaMemcpyDeviceToHost, h->s));
+            CU(h, cudaFreeAsync(tmp, h->s));
+        }
+        return CDMF_OK;
+    };
+    if ((r = down(res_csc, h->res_csc)) || (r = down(res_csr, h->res_csr))) return r;
+    CU(h, cudaStreamSynchronize(h->s));
+    if (next_oiter) *next_oiter = h->next_oiter;
+    return CDMF_OK;
+}
+
+int cdmf_cuda_set_state(cdmf_handle* h, const float* W, const float* H, const float* res_csc, const float* res_csr,
+                        int next_oiter) {
+    if (!h || !W || !H || next_oiter < 1) return CDMF_ERR_INVALID;
+    if (h->nnz > 0 && (!res_csc || !res_csr)) return CDMF_ERR_INVALID;
+    CU(h, cudaSetDevice(h->o.device));
+    CU(h, cudaMemcpyAsync(h->W, W, sizeof(float) * h->o.k * h->m, cudaMemcpyHostToDevice, h->s));
+    CU(h, cudaMemcpyAsync(h->H, H, sizeof(float) * h->o.k * h->n, cudaMemcpyHostToDevice, h->s));
+    auto upres = [&](void* dst, const float* src) -> int {
+        if (h->nnz == 0) return CDMF_OK;
+        if (h->rt == 0) {
+            CU(h, cudaMemcpyAsync(dst, src, sizeof(float) * h->nnz, cudaMemcpyHostToDevice, h->s));
+        } else {
+            float* tmp = nullptr;
+            CU(h, cudaMallocAsync((void**)&tmp, sizeof(float) * h->nnz, h->s));
+            CU(h, cudaMemcpyAsync(tmp, src, sizeof(float) * h->nnz, cudaMemcpyHostToDevice, h->s));
+            f32_to_res_kernel<<<1216, 256, 0, h->s>>>(tmp, dst, h->nnz, h->rt);
+            CU(h, cudaGetLastError());
+            CU(h, cudaFreeAsync(tmp, h->s));
+        }
+        return CDMF_OK;
+    };
+    int r;
+    if ((r = upres(h->res_csc, res_csc)) || (r = upres(h->res_csr, res_csr))) return r;
+    CU(h, cudaStreamSynchronize(h->s));
+    h->pending = -1;
+    h->next_oiter = next_oiter;
+    return CDMF_OK;
+}
+
+int cdmf_cuda_set_profiling(cdmf_handle* h, int on) {
+    if (!h) return CDMF_ERR_INVALID;
+    h->profiling = on != 0;
+    return CDMF_OK;
+}
+
+int cdmf_cuda_stats(const cdmf_handle* h, cdmf_stats* s) {
+    if (!h || !s) return CDMF_ERR_INVALID;
+    *s = h->st;
+    return CDMF_OK;
+}
+
+int cdmf_cuda_bins(const cdmf_handle* h, int which, int64_t counts[4], int64_t nnz[4]) {
+    if (!h || (which != 0 && which != 1)) return CDMF_ERR_INVALID;
+    const Bins& B = which == 0 ? h->csr.host : h->csc.host;
+    for (int q = 0; q < 4; ++q) {
+        if (counts) counts[q] = B.count[q];
+        if (nnz) nnz[q] = B.nnz[q];
+    }
+    return CDMF_OK;
+}
+
+int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* H, double* rmse_out, cdmf_outer_cb cb,
+                    void* user) {
+    if (!p || !o || !W || !H) return CDMF_ERR_INVALID;
+    cdmf_handle* h = nullptr;
+    int r = cdmf_cuda_create(p, o, &h);
+    if (r) return r;
+    if ((r = cdmf_cuda_set_factors(h, W, nullptr))) { cdmf_cuda_destroy(h); return r; }
+    const bool want_rmse = o->rmse_each_outer && p->nnz_test > 0;
+    double total_ms = 0;
+    for (int it = 0; it < o->maxiter; ++it) {
+        double rm = 0;
+        if ((r = cdmf_cuda_run(h, 1, want_rmse ? &rm : nullptr))) { cdmf_cuda_destroy(h); return r; }
+        total_ms += h->st.train_ms;
+        if (rmse_out) rmse_out[it] = want_rmse ? rm : -1.0;
+        if (cb) cb(it + 1, want_rmse ? rm : -1.0, total_ms, user);
+    }
+    h->st.train_ms = total_ms;
+    r = cdmf_cuda_get_factors(h, W, H);
+    cdmf_cuda_destroy(h);
+    return r;
+}
+
+}  // extern "C"

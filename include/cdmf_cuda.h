@@ -1,0 +1,152 @@
+/*
+ * cdmf_cuda.h -- C ABI of the GB300 (sm_103a) CCD++ engine.
+ *
+ * Drop-in for the reference's OpenCL engines (src/cdmf.h:4-10):
+ *   void cdmf_ocl_01(SparseMatrix& R, MatData& W, MatData& H, TestData& T,
+ *                    parameter& p, char filename[]);          src/cdmf.h:8
+ *   void cdmf_ocl_02(...same...);                              src/cdmf.h:6
+ *   void cdmf_csr5(SparseMatrix& R, MatData& W, MatData& H,
+ *                  parameter& p, char filename[]);             src/cdmf.h:10
+ * called from src/main.cpp:43,50,57.  The C++ types become plain pointers:
+ *   SparseMatrix (src/pmf_util.h:13-114)  -> cdmf_problem CSR + CSC arrays
+ *   TestData     (src/pmf_util.h:117-161) -> cdmf_problem test COO arrays
+ *   MatData W, H (src/pmf_util.h:8)       -> float[k*m], float[k*n], feature-major
+ *                                            (W[t*m + i] == W_c[t][i], as the
+ *                                            reference flattens it, src/cdmf_ocl_1.cpp:70-82)
+ *   parameter    (src/pmf.h:4-26)         -> cdmf_opts
+ *
+ * Semantics kept from the reference:
+ *   - host R is never modified (the GPU engines copy it, src/cdmf_ocl_1.cpp:101-133);
+ *   - W is in/out, H is output only and starts from zero (src/cdmf_ocl_1.cpp:64-68);
+ *   - the test set is read-only; the test RMSE after each outer iteration is
+ *     the value of the reference's "[-INFO-] iteration num" line
+ *     (src/cdmf_ref.cpp:130-136, src/cdmf_ocl_1.cpp:357-381).
+ * Changed on purpose: errors are returned as negative status codes instead of
+ * abort()/exit() (src/util.h:20-22, src/main.cpp:60-63); the library never
+ * terminates the process.
+ *
+ * Threading: a handle belongs to the thread that uses it; distinct handles
+ * may be used from distinct threads.  All pointers passed to create/train are
+ * borrowed for the duration of the call only.
+ */
+#ifndef CDMF_CUDA_H
+#define CDMF_CUDA_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes: 0 = OK, negative = error. */
+#define CDMF_OK 0
+#define CDMF_ERR_INVALID (-1)      /* bad argument or inconsistent sparse structure */
+#define CDMF_ERR_ALLOC (-2)        /* host or device allocation failed */
+#define CDMF_ERR_CUDA (-3)         /* CUDA runtime error (see cdmf_cuda_last_error) */
+#define CDMF_ERR_NO_DEVICE (-4)    /* no usable CUDA device */
+#define CDMF_ERR_EMPTY_TEST (-5)   /* RMSE asked for with an empty test set (src/tools.cpp:576 exits) */
+#define CDMF_ERR_NUMERIC (-6)      /* residual drift / non-finite factors reported by a device check */
+#define CDMF_ERR_UNSUPPORTED (-7)  /* option combination not supported */
+#define CDMF_ERR_TOO_LARGE (-8)    /* size beyond a stated limit */
+
+/* Residual storage precision (cdmf_opts.residual). */
+#define CDMF_RES_F32 0
+#define CDMF_RES_BF16 1
+#define CDMF_RES_F16 2
+
+/* Reduction order (cdmf_opts.reduce). */
+#define CDMF_REDUCE_TREE 0        /* parallel, deterministic fixed-shape tree */
+#define CDMF_REDUCE_SEQUENTIAL 1  /* every line summed by one thread in index order:
+                                     the reference's order (src/cdmf_ref.cpp:10-14) */
+
+/* SparseMatrix + TestData (src/pmf_util.h:13-161) as plain arrays.
+ * CSR: csr_row_ptr[m+1], csr_col_idx[nnz], csr_val[nnz];
+ * CSC: csc_col_ptr[n+1], csc_row_idx[nnz], csc_val[nnz] -- the same matrix;
+ * indices inside a line ascending (scipy canonical order).
+ * Test COO: test_row/test_col/test_val[nnz_test], 0-based. */
+typedef struct {
+    int64_t m, n, nnz;
+    const uint32_t *csr_row_ptr, *csr_col_idx;
+    const float *csr_val;
+    const uint32_t *csc_col_ptr, *csc_row_idx;
+    const float *csc_val;
+    int64_t nnz_test;
+    const uint32_t *test_row, *test_col;
+    const float *test_val;
+} cdmf_problem;
+
+/* parameter (src/pmf.h:4-26) plus the engine's own knobs. */
+typedef struct {
+    uint32_t k;               /* rank (-k, default 10) */
+    float lambda;             /* regularisation (-l, default 0.1) */
+    int32_t maxiter;          /* outer iterations (-t, default 5) */
+    int32_t maxinneriter;     /* inner iterations (-T, default 5) */
+    int32_t version;          /* -V: 1 and 2 = row-length-binned sweeps, 3 = nnz-balanced tiles */
+    int32_t residual;         /* CDMF_RES_* */
+    int32_t reduce;           /* CDMF_REDUCE_* */
+    int32_t rmse_each_outer;  /* 1: test RMSE after every outer iteration, as the reference */
+    int32_t use_graph;        /* 1: replay each outer iteration as one CUDA graph */
+    int32_t threads_per_block;/* -nThreadsPerBlock; 0 = engine default (256) */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t verbose;
+} cdmf_opts;
+
+/* Engine timings and counters of the most recent cdmf_cuda_run/train. */
+typedef struct {
+    double train_ms;          /* CUDA-event time of the whole run on the engine stream */
+    double sweep_csc_ms;      /* sum of CSC (h_t) sweep kernel times   (profiling on) */
+    double sweep_csr_ms;      /* sum of CSR (w_t) sweep kernel times   (profiling on) */
+    double rmse_ms;           /* sum of test-RMSE kernel times         (profiling on) */
+    double refresh_ms;        /* sum of residual refresh kernel times  (profiling on) */
+    int64_t launches;         /* kernels launched by the run */
+    int64_t sweep_csc_launches, sweep_csr_launches, rmse_launches, refresh_launches;
+    int64_t updates;          /* rank-one updates performed (outer iterations x k) */
+    double bytes_per_update;  /* compulsory HBM bytes of one rank-one update (see DESIGN) */
+} cdmf_stats;
+
+typedef struct cdmf_handle cdmf_handle;
+
+/* Called after every outer iteration: the reference's log-line values. */
+typedef void (*cdmf_outer_cb)(int oiter, double rmse, double train_ms_so_far, void* user);
+
+void cdmf_opts_default(cdmf_opts* o);
+const char* cdmf_cuda_strerror(int status);
+int cdmf_cuda_version(void);
+
+/* One call = the reference engine call (cdmf_ocl_01 / cdmf_ocl_02 / cdmf_csr5):
+ * upload, H := 0, maxiter outer iterations from the given W, download W and H.
+ * rmse_out (nullable) receives maxiter values when opts->rmse_each_outer. */
+int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* H,
+                    double* rmse_out, cdmf_outer_cb cb, void* user);
+
+/* Handle API: the same engine split into upload / run / read-back. */
+int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** out);
+void cdmf_cuda_destroy(cdmf_handle* h);
+const char* cdmf_cuda_last_error(const cdmf_handle* h);
+/* Starts a fresh factorisation: W := W0, H := H0 (NULL = zero, as the
+ * reference), both residual copies := the ratings, next outer iteration = 1. */
+int cdmf_cuda_set_factors(cdmf_handle* h, const float* W0, const float* H0);
+/* Runs n_outer further outer iterations.  rmse_out (nullable) gets one value
+ * per iteration when rmse_each_outer is set. */
+int cdmf_cuda_run(cdmf_handle* h, int n_outer, double* rmse_out);
+int cdmf_cuda_get_factors(cdmf_handle* h, float* W, float* H);
+/* Test RMSE of the current factors (src/tools.cpp:543-582). */
+int cdmf_cuda_rmse(cdmf_handle* h, double* rmse);
+/* Full engine state for one-step parity: factors, both residual copies (in
+ * CSC and CSR order, widened to float) and the next outer iteration number. */
+int cdmf_cuda_get_state(cdmf_handle* h, float* W, float* H, float* res_csc, float* res_csr, int* next_oiter);
+int cdmf_cuda_set_state(cdmf_handle* h, const float* W, const float* H, const float* res_csc,
+                        const float* res_csr, int next_oiter);
+int cdmf_cuda_set_profiling(cdmf_handle* h, int on);
+int cdmf_cuda_stats(const cdmf_handle* h, cdmf_stats* s);
+/* Page-locked host memory for inputs and outputs of cdmf_cuda_train /
+ * create / get_factors (copies from it run at full link speed).  NULL on
+ * failure. */
+void* cdmf_cuda_host_alloc(uint64_t bytes);
+void cdmf_cuda_host_free(void* p);
+/* Row-length bins of the two sweeps: counts[4] of lines per bin
+ * (thread, warp, CTA, split) and nnz[4] for CSR (which=0) or CSC (which=1). */
+int cdmf_cuda_bins(const cdmf_handle* h, int which, int64_t counts[4], int64_t nnz[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,140 @@
+"""ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+liboracle_f32.so / liboracle_f64.so: the C restatement of the reference's
+CCD++ engine (oracle/ccdpp_oracle.c).  _ref/libcdmf_ref.so: the reference's
+own src/cdmf_ref.cpp + src/tools.cpp (oracle/build_ref.sh), present only
+where the reference sources are.  Only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg use this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_LIB = os.path.join(HERE, "_ref", "libcdmf_ref.so")
+
+
+class OracleProblem(ctypes.Structure):
+    _fields_ = [
+        ("m", ctypes.c_int64), ("n", ctypes.c_int64), ("nnz", ctypes.c_int64),
+        ("csr_row_ptr", ctypes.c_void_p), ("csr_col_idx", ctypes.c_void_p), ("csr_val", ctypes.c_void_p),
+        ("csc_col_ptr", ctypes.c_void_p), ("csc_row_idx", ctypes.c_void_p), ("csc_val", ctypes.c_void_p),
+        ("nnz_test", ctypes.c_int64),
+        ("test_row", ctypes.c_void_p), ("test_col", ctypes.c_void_p), ("test_val", ctypes.c_void_p),
+    ]
+
+
+def build():
+    """Compiles liboracle_f32/f64 (and oracle/_ref when the reference is present)."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    subprocess.check_call([os.path.join(HERE, "build_ref.sh")], stdout=subprocess.DEVNULL)
+
+
+_LIBS = {}
+
+
+def _lib(dtype):
+    key = np.dtype(dtype).name
+    if key not in _LIBS:
+        path = os.path.join(HERE, "liboracle_f32.so" if key == "float32" else "liboracle_f64.so")
+        if not os.path.exists(path):
+            build()
+        lib = ctypes.CDLL(path)
+        vp, i, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        lib.oracle_ccdpp.argtypes = [ctypes.POINTER(OracleProblem), ctypes.c_uint32, d, i, i, i, vp, vp, vp, vp, vp,
+                                     vp, vp, vp]
+        lib.oracle_ccdpp.restype = i
+        lib.oracle_outer_iteration.argtypes = [ctypes.POINTER(OracleProblem), ctypes.c_uint32, d, i, i, i, vp, vp,
+                                               vp, vp, vp, vp]
+        lib.oracle_outer_iteration.restype = i
+        lib.oracle_rmse.argtypes = [ctypes.POINTER(OracleProblem), ctypes.c_uint32, vp, vp]
+        lib.oracle_rmse.restype = d
+        _LIBS[key] = lib
+    return _LIBS[key]
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def problem(R):
+    """OracleProblem over a RatingMatrix (arrays must stay alive)."""
+    return OracleProblem(R.m, R.n, R.nnz, _p(R.csr_ptr), _p(R.csr_idx), _p(R.csr_val), _p(R.csc_ptr),
+                         _p(R.csc_idx), _p(R.csc_val), R.nnz_test, _p(R.te_row), _p(R.te_col), _p(R.te_val))
+
+
+def ccdpp(R, W0, k, lam, maxiter, maxinner, threads=0, dtype=np.float32, history=False, residuals=False):
+    """Runs the oracle engine.  Returns dict(W, H, rmse[maxiter], times, [W_hist, H_hist], [res_csc, res_csr])."""
+    lib = _lib(dtype)
+    P = problem(R)
+    W = np.ascontiguousarray(W0, dtype=dtype).copy()
+    H = np.zeros((k, R.n), dtype=dtype)
+    rmse = np.zeros(max(1, maxiter), np.float64)
+    times = np.zeros(2 * max(1, maxiter), np.float64)
+    Wh = np.zeros((maxiter, k, R.m), dtype) if history else None
+    Hh = np.zeros((maxiter, k, R.n), dtype) if history else None
+    rc = np.zeros(R.nnz, dtype) if residuals else None
+    rr = np.zeros(R.nnz, dtype) if residuals else None
+    st = lib.oracle_ccdpp(ctypes.byref(P), k, lam, maxiter, maxinner, threads, _p(W), _p(H), _p(rmse), _p(Wh),
+                          _p(Hh), _p(rc), _p(rr), _p(times))
+    if st != 0:
+        raise RuntimeError("oracle_ccdpp failed")
+    out = dict(W=W, H=H, rmse=rmse[:maxiter], times=times[:2 * maxiter].reshape(-1, 2))
+    if history:
+        out.update(W_hist=Wh, H_hist=Hh)
+    if residuals:
+        out.update(res_csc=rc, res_csr=rr)
+    return out
+
+
+def outer_iteration(R, W, H, res_csc, res_csr, k, lam, maxinner, oiter, threads=0):
+    """One outer iteration in place on an explicit state (float32 or float64 arrays)."""
+    lib = _lib(W.dtype)
+    P = problem(R)
+    st = lib.oracle_outer_iteration(ctypes.byref(P), k, lam, maxinner, oiter, threads, _p(W), _p(H), _p(res_csc),
+                                    _p(res_csr), None, None)
+    if st != 0:
+        raise RuntimeError("oracle_outer_iteration failed")
+
+
+def rmse(R, W, H, k):
+    lib = _lib(W.dtype)
+    P = problem(R)
+    return lib.oracle_rmse(ctypes.byref(P), k, _p(W), _p(H))
+
+
+def reference_available():
+    return os.path.exists(REF_LIB)
+
+
+def reference_run(data_dir, W0, k, lam, maxiter, maxinner, threads=1, residuals=False):
+    """The reference's own cdmf_ref on a cdmf-format directory (oracle/_ref)."""
+    lib = ctypes.CDLL(REF_LIB)
+    m, n = ctypes.c_long(), ctypes.c_long()
+    nnz, nt = ctypes.c_ulong(), ctypes.c_ulong()
+    lib.ref_dims(data_dir.encode(), ctypes.byref(m), ctypes.byref(n), ctypes.byref(nnz), ctypes.byref(nt))
+    W0 = np.ascontiguousarray(W0, np.float32)
+    W = np.zeros((k, m.value), np.float32)
+    H = np.zeros((k, n.value), np.float32)
+    r = ctypes.c_double()
+    rc = np.zeros(nnz.value, np.float32) if residuals else None
+    rr = np.zeros(nnz.value, np.float32) if residuals else None
+    lib.ref_run.argtypes = [ctypes.c_char_p, ctypes.c_uint, ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                            ctypes.c_void_p]
+    lib.ref_run(data_dir.encode(), k, lam, maxiter, maxinner, threads, _p(W0), _p(W), _p(H), ctypes.addressof(r),
+                _p(rc), _p(rr))
+    out = dict(W=W, H=H, rmse=r.value)
+    if residuals:
+        out.update(res_csc=rc, res_csr=rr)
+    return out
+
+
+def reference_initial_col(k, n):
+    lib = ctypes.CDLL(REF_LIB)
+    X = np.zeros((k, n), np.float32)
+    lib.ref_initial_col.argtypes = [ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint]
+    lib.ref_initial_col(_p(X), k, n)
+    return X

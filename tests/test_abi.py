@@ -1,0 +1,83 @@
+"""The C ABI library: loads, exports every declared entry point, rejects bad
+input on the host (no GPU work in these tests)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden
+from cdmf_gb300 import _lib, engine
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for line in text.split(";"):
+            line = " ".join(line.split())
+            if line.startswith("typedef") or "#define" in line:
+                continue
+            mt = re.search(r"\b(cdmf_\w+)\s*\(", line)
+            if mt:
+                names.add(mt.group(1))
+    return names
+
+
+def test_library_exports_declared_symbols():
+    lib = _lib.load()
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _lib.EXPORTS, n
+
+
+def test_strerror_and_defaults():
+    lib = _lib.load()
+    assert lib.cdmf_cuda_strerror(0) == b"ok"
+    assert lib.cdmf_cuda_strerror(-1).startswith(b"invalid")
+    o = _lib.Opts()
+    lib.cdmf_opts_default(ctypes.byref(o))
+    assert (o.k, o.maxiter, o.maxinneriter) == (10, 5, 5) and abs(o.lambda_ - 0.1) < 1e-7
+
+
+def _create(R, **kw):
+    o = engine.make_opts(kw.pop("k", 4), kw.pop("lambda_", 0.1), **kw)
+    p = engine._problem(R)
+    h = ctypes.c_void_p()
+    st = _lib.load().cdmf_cuda_create(ctypes.byref(p), ctypes.byref(o), ctypes.byref(h))
+    if st == 0:
+        _lib.load().cdmf_cuda_destroy(h)
+    return st
+
+
+def test_create_rejects_bad_structures():
+    R, _ = load_golden("simple")
+    bad = load_golden("simple")[0]
+    bad.csr_idx = R.csr_idx.copy()
+    bad.csr_idx[3] = 99                                   # column out of range
+    assert _create(bad) == -1
+    bad = load_golden("simple")[0]
+    bad.csc_ptr = R.csc_ptr.copy()
+    bad.csc_ptr[2], bad.csc_ptr[3] = bad.csc_ptr[3], bad.csc_ptr[2]   # not monotone
+    assert _create(bad) == -1
+    bad = load_golden("simple")[0]
+    bad.te_row = R.te_row.copy()
+    bad.te_row[0] = 6                                     # test row out of range
+    assert _create(bad) == -1
+    assert _create(R, k=0) == -1
+    assert _create(R, lambda_=-1.0) == -1
+    assert _create(R, residual=5) == -1
+
+
+def test_null_arguments():
+    lib = _lib.load()
+    assert lib.cdmf_cuda_create(None, None, None) == -1
+    assert lib.cdmf_cuda_run(None, 1, None) == -1
+    assert lib.cdmf_cuda_get_factors(None, None, None) == -1
+    lib.cdmf_cuda_destroy(None)

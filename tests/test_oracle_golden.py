@@ -1,0 +1,86 @@
+"""The CPU oracle against golden vectors produced by the reference's own
+engine (tests/golden/make_golden.py runs src/cdmf_ref.cpp unmodified)."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_golden
+from oracle import oracle
+
+META = json.load(open(os.path.join(GOLDEN, "golden.json")))
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32 if a.dtype == np.float32 else np.uint64)
+
+
+@pytest.mark.parametrize("name", ["simple", "tricky_simple", "mini"])
+def test_oracle_bit_exact_vs_reference(name):
+    R, z = load_golden(name)
+    md = META[name]
+    out = oracle.ccdpp(R, z["W0"], md["k"], md["lam"], md["maxiter"], md["maxinner"], threads=2, history=True,
+                       residuals=True)
+    assert np.array_equal(bits(out["W_hist"]), bits(z["W_hist"]))
+    assert np.array_equal(bits(out["H_hist"]), bits(z["H_hist"]))
+    assert np.array_equal(bits(out["res_csc"]), bits(z["res_csc"]))
+    assert np.array_equal(bits(out["res_csr"]), bits(z["res_csr"]))
+    assert np.array_equal(out["rmse"], z["rmse"])
+
+
+def test_simple_known_values():
+    # data/simple with the reference's ctest flags: the values the reference prints
+    md = META["simple"]
+    assert abs(md["rmse"][-1] - 0.097691) < 5e-7
+    _, z = load_golden("simple")
+    assert abs(float(z["W_hist"][-1][0][0]) - 1.35162961) < 1e-7
+    assert abs(META["tricky_simple"]["rmse"][-1] - 1.225676) < 5e-7
+
+
+def test_oracle_cpu_scale_digest():
+    from golden.make_golden import matrix_digest  # noqa: F401  (same digest definition)
+    from cdmf_gb300 import synth
+    md = META["cpu_scale"]
+    R, run = synth.config("cpu_scale")
+    if matrix_digest(R) != md["matrix_sha256"]:
+        pytest.skip("generator output differs on this host's libm; digests do not apply")
+    W0 = synth.initial_w(md["k"], R.m, seed=0)
+    out = oracle.ccdpp(R, W0, md["k"], md["lam"], md["maxiter"], md["maxinner"], threads=4, history=True)
+    assert [hashlib.sha256(w.tobytes()).hexdigest() for w in out["W_hist"]] == md["W_sha256"]
+    assert [hashlib.sha256(h.tobytes()).hexdigest() for h in out["H_hist"]] == md["H_sha256"]
+    assert np.array_equal(out["rmse"], np.array(md["rmse"]))
+
+
+def test_oracle_thread_invariance():
+    R, z = load_golden("mini")
+    md = META["mini"]
+    a = oracle.ccdpp(R, z["W0"], md["k"], md["lam"], 2, md["maxinner"], threads=1)
+    b = oracle.ccdpp(R, z["W0"], md["k"], md["lam"], 2, md["maxinner"], threads=4)
+    assert np.array_equal(bits(a["W"]), bits(b["W"])) and np.array_equal(bits(a["H"]), bits(b["H"]))
+
+
+def test_outer_iteration_composes():
+    # running outer iterations one at a time from the state equals one run
+    R, z = load_golden("mini")
+    md = META["mini"]
+    k = md["k"]
+    W = z["W0"].copy()
+    H = np.zeros((k, R.n), np.float32)
+    rc, rr = R.csc_val.copy(), R.csr_val.copy()
+    for j in range(1, md["maxiter"] + 1):
+        oracle.outer_iteration(R, W, H, rc, rr, k, md["lam"], md["maxinner"], j, threads=2)
+        assert np.array_equal(bits(W), bits(z["W_hist"][j - 1]))
+        assert np.array_equal(bits(H), bits(z["H_hist"][j - 1]))
+    assert np.array_equal(bits(rc), bits(z["res_csc"]))
+
+
+def test_fp64_oracle_tracks_fp32():
+    R, z = load_golden("mini")
+    md = META["mini"]
+    a = oracle.ccdpp(R, z["W0"], md["k"], md["lam"], md["maxiter"], md["maxinner"], dtype=np.float32)
+    b = oracle.ccdpp(R, z["W0"].astype(np.float64), md["k"], md["lam"], md["maxiter"], md["maxinner"],
+                     dtype=np.float64)
+    assert np.max(np.abs(a["rmse"] - b["rmse"])) < 1e-4
+    assert np.max(np.abs(a["W"] - b["W"])) < 1e-3 * np.max(np.abs(b["W"]))

@@ -1,0 +1,182 @@
+"""CUDA engine vs the oracle and the reference's golden vectors.
+
+Two reduction modes:
+  sequential -- every line is summed by one thread in index order, the
+                reference's order: results must be BIT-EXACT after every outer
+                iteration (W, H, both residual copies) and the RMSE equal;
+  tree       -- the production mode (warp / CTA / split-line trees):
+                W and H within a relative 1e-5 of the reference after each
+                outer iteration, test RMSE within 1e-5 absolute.
+Relative error of x against x_ref: |x - x_ref| <= 1e-5 * max(|x_ref|, 0.1 * rms(x_ref_t))
+elementwise, where rms(x_ref_t) is the RMS of that feature's vector (the
+floor keeps entries that cancel to near zero from demanding more than FP32
+summation can give).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_golden
+from cdmf_gb300 import engine, synth
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+META = json.load(open(os.path.join(GOLDEN, "golden.json")))
+RTOL = 1e-5
+RMSE_ATOL = 1e-5
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def rel_ok(x, ref, rtol=RTOL):
+    x = np.asarray(x, np.float64).reshape(ref.shape[0], -1)
+    ref = np.asarray(ref, np.float64).reshape(ref.shape[0], -1)
+    rms = np.sqrt(np.mean(ref * ref, axis=1, keepdims=True))
+    scale = np.maximum(np.abs(ref), 0.1 * rms)
+    err = np.abs(x - ref) / np.where(scale > 0, scale, 1.0)
+    return float(err.max()) <= rtol, float(err.max())
+
+
+@pytest.mark.parametrize("name", ["simple", "tricky_simple", "mini"])
+def test_sequential_bit_exact_each_outer(name):
+    R, z = load_golden(name)
+    md = META[name]
+    with engine.Engine(R, md["k"], md["lam"], md["maxiter"], md["maxinner"], reduce="sequential") as e:
+        e.set_factors(z["W0"])
+        for j in range(md["maxiter"]):
+            rm = e.run(1)
+            W, H = e.factors()
+            assert np.array_equal(bits(W), bits(z["W_hist"][j])), f"W after outer {j + 1}"
+            assert np.array_equal(bits(H), bits(z["H_hist"][j])), f"H after outer {j + 1}"
+            assert abs(rm[0] - z["rmse"][j]) <= 1e-12
+        st = e.state()
+    assert np.array_equal(bits(st["res_csc"]), bits(z["res_csc"]))
+    assert np.array_equal(bits(st["res_csr"]), bits(z["res_csr"]))
+
+
+@pytest.mark.parametrize("name", ["simple", "tricky_simple", "mini"])
+def test_tree_within_tolerance_each_outer(name):
+    R, z = load_golden(name)
+    md = META[name]
+    with engine.Engine(R, md["k"], md["lam"], md["maxiter"], md["maxinner"]) as e:
+        e.set_factors(z["W0"])
+        for j in range(md["maxiter"]):
+            rm = e.run(1)
+            W, H = e.factors()
+            okw, ew = rel_ok(W, z["W_hist"][j])
+            okh, eh = rel_ok(H, z["H_hist"][j])
+            assert okw and okh, (j, ew, eh)
+            assert abs(rm[0] - z["rmse"][j]) <= RMSE_ATOL
+
+
+def test_one_shot_train_matches_handle_api():
+    R, z = load_golden("mini")
+    md = META["mini"]
+    W, H, rm = engine.train(R, z["W0"], md["k"], md["lam"], md["maxiter"], md["maxinner"], reduce="sequential")
+    assert np.array_equal(bits(W), bits(z["W_hist"][-1])) and np.array_equal(bits(H), bits(z["H_hist"][-1]))
+    assert np.max(np.abs(rm - z["rmse"])) <= 1e-12
+
+
+@pytest.fixture(scope="module")
+def cpu_scale():
+    R, run = synth.config("cpu_scale")
+    W0 = synth.initial_w(run["k"], R.m, seed=0)
+    ref = oracle.ccdpp(R, W0, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"], threads=8,
+                       history=True, residuals=True)
+    return R, run, W0, ref
+
+
+def test_cpu_scale_sequential_bit_exact(cpu_scale):
+    R, run, W0, ref = cpu_scale
+    with engine.Engine(R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"], reduce="sequential") as e:
+        e.set_factors(W0)
+        for j in range(run["maxiter"]):
+            rm = e.run(1)
+            W, H = e.factors()
+            assert np.array_equal(bits(W), bits(ref["W_hist"][j])) and np.array_equal(bits(H), bits(ref["H_hist"][j]))
+            assert abs(rm[0] - ref["rmse"][j]) <= 1e-12
+        st = e.state()
+    assert np.array_equal(bits(st["res_csc"]), bits(ref["res_csc"]))
+    assert np.array_equal(bits(st["res_csr"]), bits(ref["res_csr"]))
+
+
+def test_cpu_scale_tree_one_step_parity(cpu_scale):
+    """From the oracle's state after outer j, one GPU outer iteration lands
+    within tolerance of the oracle's outer j+1 (errors do not compound)."""
+    R, run, W0, ref = cpu_scale
+    k, lam, T = run["k"], run["lambda_"], run["maxinneriter"]
+    W = W0.copy()
+    H = np.zeros((k, R.n), np.float32)
+    rc, rr = R.csc_val.copy(), R.csr_val.copy()
+    with engine.Engine(R, k, lam, run["maxiter"], T) as e:
+        for j in range(1, run["maxiter"] + 1):
+            e.set_state(W, H, rc, rr, j)
+            rm = e.run(1)
+            Wg, Hg = e.factors()
+            oracle.outer_iteration(R, W, H, rc, rr, k, lam, T, j, threads=8)
+            okw, ew = rel_ok(Wg, W)
+            okh, eh = rel_ok(Hg, H)
+            assert okw and okh, (j, ew, eh)
+            assert abs(rm[0] - oracle.rmse(R, W, H, k)) <= RMSE_ATOL
+
+
+def test_cpu_scale_tree_free_running(cpu_scale):
+    R, run, W0, ref = cpu_scale
+    with engine.Engine(R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"]) as e:
+        e.set_factors(W0)
+        rm = e.run(run["maxiter"])
+        W, H = e.factors()
+    assert np.max(np.abs(rm - ref["rmse"])) <= RMSE_ATOL, (rm, ref["rmse"])
+    okw, ew = rel_ok(W, ref["W"], rtol=1e-4)
+    okh, eh = rel_ok(H, ref["H"], rtol=1e-4)
+    assert okw and okh, (ew, eh)
+
+
+@pytest.mark.parametrize("k,T", [(1, 3), (3, 1), (2, 2)])
+def test_small_rank_and_inner_counts_bit_exact(k, T):
+    R, z = load_golden("mini")
+    W0 = synth.initial_w(k, R.m, seed=5)
+    ref = oracle.ccdpp(R, W0, k, 0.1, 3, T, history=True, residuals=True)
+    with engine.Engine(R, k, 0.1, 3, T, reduce="sequential") as e:
+        e.set_factors(W0)
+        rm = e.run(3)
+        st = e.state()
+    assert np.array_equal(bits(st["W"]), bits(ref["W"])) and np.array_equal(bits(st["H"]), bits(ref["H"]))
+    assert np.array_equal(bits(st["res_csc"]), bits(ref["res_csc"]))
+    assert np.array_equal(bits(st["res_csr"]), bits(ref["res_csr"]))
+    assert np.max(np.abs(rm - ref["rmse"])) <= 1e-12
+
+
+def test_state_roundtrip_continues_identically():
+    R, z = load_golden("mini")
+    md = META["mini"]
+    with engine.Engine(R, md["k"], md["lam"], md["maxiter"], md["maxinner"], reduce="sequential") as e:
+        e.set_factors(z["W0"])
+        e.run(2)
+        st = e.state()            # flushes the pending subtract
+        e.set_state(st["W"], st["H"], st["res_csc"], st["res_csr"], st["next_oiter"])
+        e.run(2)
+        W, H = e.factors()
+    assert np.array_equal(bits(W), bits(z["W_hist"][3])) and np.array_equal(bits(H), bits(z["H_hist"][3]))
+
+
+def test_split_lines_bit_exact_in_sequential_and_close_in_tree():
+    # a matrix with very long columns exercises the split-line bin (> 16384 nnz)
+    R = synth.generate(m=60000, n=40, nnz_total=900000, test_fraction=0.01, row_alpha=0.5, row_min=1, row_max=40,
+                       col_alpha=0.3, col_cap=60000, rank=4, seed=21)
+    W0 = synth.initial_w(4, R.m, seed=1)
+    ref = oracle.ccdpp(R, W0, 4, 0.05, 2, 2, threads=8, history=True)
+    with engine.Engine(R, 4, 0.05, 2, 2) as e:
+        c, _ = e.bins("csc")
+        assert c[3] > 0, c
+        e.set_factors(W0)
+        rm = e.run(1)
+        W, H = e.factors()
+    okw, ew = rel_ok(W, ref["W_hist"][0])
+    okh, eh = rel_ok(H, ref["H_hist"][0])
+    assert okw and okh, (ew, eh)
+    assert abs(rm[0] - ref["rmse"][0]) <= RMSE_ATOL
