@@ -171,6 +171,7 @@ def main():
     ap.add_argument("--e2e-outer", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="device-resident timing only (no e2e, no CPU leg)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     args.warmup = max(3, args.warmup)
@@ -249,30 +250,11 @@ def main():
     test_rmse = float(rm[-1]) if rm is not None else None
     e.close()
 
-    # e2e through the one-shot engine call from page-locked host memory
-    arrays = {}
-    owners = []
-    for name in ("csr_ptr", "csr_idx", "csr_val", "csc_ptr", "csc_idx", "csc_val", "te_row", "te_col", "te_val"):
-        src = getattr(R, name)
-        a, o = _lib.pinned_empty(src.shape, src.dtype)
-        a[...] = src
-        arrays[name] = a
-        owners.append(o)
-    from cdmf_gb300.formats import RatingMatrix
-    Rp = RatingMatrix(R.m, R.n, **arrays)
-    Wp, ow = _lib.pinned_empty(W0.shape, np.float32)
-    owners.append(ow)
-    h2d = sum(getattr(Rp, f).nbytes for f in arrays) + W0.nbytes
-    d2h = W0.nbytes + 4 * k * R.n + 8 * args.e2e_outer
-    Wp[...] = W0
-    engine.train(Rp, Wp, k, lam, 1, T, residual=args.residual, device=device)  # warm the context
-    dist.barrier()
-    t0 = time.perf_counter()
-    Wp[...] = W0
-    _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, residual=args.residual, device=device)
-    e2e_s = dist.max(time.perf_counter() - t0)
-    e2e_value = ws * k * args.e2e_outer / e2e_s
-
+    if args.quick:
+        args.no_cpu = True
+    e2e = None
+    if not args.quick:
+        e2e = run_e2e(R, W0, k, lam, T, args, dist, ws, device)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         v, f, s = cpu_sample(R, run, W0, threads, args.cpu_budget)
@@ -302,12 +284,40 @@ def main():
                      "traffic": traffic, "peak_source": peak_kind,
                      "kernel": "sweep_kernel (CSC h-sweep + CSR w-sweep)",
                      "bytes_per_launch": bytes_launch, "mean_launch_ms": mean_launch_s * 1e3},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "step": f"one cdmf_cuda_train call: upload, {args.e2e_outer} outer iterations, download",
-                "seconds": e2e_s, "test_rmse": float(e2e_rm[-1])},
+        "e2e": e2e,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
+
+
+def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
+    """updates/s through cdmf_cuda_train from page-locked host buffers."""
+    from cdmf_gb300 import engine, _lib
+    from cdmf_gb300.formats import RatingMatrix
+    arrays = {}
+    owners = []
+    for name in ("csr_ptr", "csr_idx", "csr_val", "csc_ptr", "csc_idx", "csc_val", "te_row", "te_col", "te_val"):
+        src = getattr(R, name)
+        a, o = _lib.pinned_empty(src.shape, src.dtype)
+        a[...] = src
+        arrays[name] = a
+        owners.append(o)
+    Rp = RatingMatrix(R.m, R.n, **arrays)
+    Wp, ow = _lib.pinned_empty(W0.shape, np.float32)
+    owners.append(ow)
+    h2d = sum(getattr(Rp, f).nbytes for f in arrays) + W0.nbytes
+    d2h = W0.nbytes + 4 * k * R.n + 8 * args.e2e_outer
+    Wp[...] = W0
+    engine.train(Rp, Wp, k, lam, 1, T, residual=args.residual, device=device)  # warm the context
+    dist.barrier()
+    t0 = time.perf_counter()
+    Wp[...] = W0
+    _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, residual=args.residual, device=device)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = ws * k * args.e2e_outer / e2e_s
+    return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "step": f"one cdmf_cuda_train call: upload, {args.e2e_outer} outer iterations, download",
+            "seconds": e2e_s, "test_rmse": float(e2e_rm[-1])}
 
 
 if __name__ == "__main__":

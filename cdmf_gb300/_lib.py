@@ -48,7 +48,7 @@ class Stats(ctypes.Structure):
         ("rmse_ms", ctypes.c_double), ("refresh_ms", ctypes.c_double), ("launches", ctypes.c_int64),
         ("sweep_csc_launches", ctypes.c_int64), ("sweep_csr_launches", ctypes.c_int64),
         ("rmse_launches", ctypes.c_int64), ("refresh_launches", ctypes.c_int64), ("updates", ctypes.c_int64),
-        ("bytes_per_update", ctypes.c_double),
+        ("bytes_per_update", ctypes.c_double), ("drift_rms", ctypes.c_double), ("nonfinite", ctypes.c_int64),
     ]
 
 
@@ -74,6 +74,8 @@ EXPORTS = {
     "cdmf_cuda_version": (ctypes.c_int, []),
     "cdmf_cuda_train": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Opts), c_f32p, c_f32p, c_f64p,
                                        OUTER_CB, ctypes.c_void_p]),
+    "cdmf_cuda_rmse_coo": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_int64, ctypes.c_int64, c_f32p, c_f32p,
+                                          ctypes.c_int64, c_u32p, c_u32p, c_f64p, ctypes.c_int, c_f64p, c_i64p]),
     "cdmf_cuda_create": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Opts),
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "cdmf_cuda_destroy": (None, [ctypes.c_void_p]),

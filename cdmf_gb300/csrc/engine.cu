@@ -13,15 +13,18 @@
 //
 // The reference reads W[t], H[t] into u, v and writes them back after the
 // inner loop (src/cdmf_ref.cpp:80-83,115-118).  Here the CSC sweep overwrites
-// H[t] in place and keeps the old H[t] in `hsave` (the CSR add-back needs it);
-// the CSR sweep overwrites W[t] in place (each row reads only its own old
-// w_i before writing it).
+// H[t] in place and forwards the old H[t] (which the CSR add-back needs) in
+// the packed table Q; the CSR sweep overwrites W[t] in place (each row reads
+// only its own old w_i before writing it) and writes the packed table P the
+// next feature's CSC sweep gathers from.
 #include "../../include/cdmf_cuda.h"
 #include "sweep_kernels.cuh"
+#include "refresh_kernels.cuh"
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -113,13 +116,25 @@ struct cdmf_handle {
     uint32_t *csr_ptr = nullptr, *csr_idx = nullptr, *csc_ptr = nullptr, *csc_idx = nullptr;
     float *csr_val = nullptr, *csc_val = nullptr;  // pristine ratings
     void *res_csr = nullptr, *res_csc = nullptr;   // residual copies
-    float *W = nullptr, *H = nullptr, *hsave = nullptr;
+    float *W = nullptr, *H = nullptr;
+    float2* P = nullptr;             // packed CSC gather table (m)
+    float4* Q = nullptr;             // packed CSR gather table (n)
+    int p_for = -1;                  // feature whose CSC sweep P is valid for
     uint32_t *te_row = nullptr, *te_col = nullptr;
     float* te_val = nullptr;
     double *rmse_part = nullptr, *rmse_out = nullptr;
     uint32_t* rmse_count = nullptr;
     int rmse_grid = 0;
     DevBins csr, csc;
+    // 16-bit residual modes: CSR->CSC position map, row-major factor copies
+    uint32_t* to_csc = nullptr;
+    float *Wrm = nullptr, *Hrm = nullptr;
+    uint32_t kp = 0;
+    int ref_grid = 0;
+    double *ref_part = nullptr, *drift_out = nullptr;
+    uint32_t* ref_count = nullptr;
+    unsigned long long* nonfinite = nullptr;
+    bool refreshed = false;
     // state
     int next_oiter = 1;
     int pending = -1;                // feature whose subtract is still owed, -1 = none
@@ -229,28 +244,28 @@ struct Timed {
     }
 };
 
-template <int RT>
-void launch_sweep_rt(const SweepArgs& A, bool sub, bool add, unsigned grid, cudaStream_t s) {
-    if (sub && add) sweep_kernel<RT, true, true><<<grid, kBlock, 0, s>>>(A);
-    else if (sub) sweep_kernel<RT, true, false><<<grid, kBlock, 0, s>>>(A);
-    else if (add) sweep_kernel<RT, false, true><<<grid, kBlock, 0, s>>>(A);
-    else sweep_kernel<RT, false, false><<<grid, kBlock, 0, s>>>(A);
+template <int RT, int MODE>
+void launch_mode(const SweepArgs& A, bool sub, bool add, unsigned grid, cudaStream_t s) {
+    if (MODE == M_PLAIN) sweep_kernel<RT, M_PLAIN, false, false><<<grid, kBlock, 0, s>>>(A);
+    else if (sub && add) sweep_kernel<RT, MODE, true, true><<<grid, kBlock, 0, s>>>(A);
+    else if (sub) sweep_kernel<RT, MODE, true, false><<<grid, kBlock, 0, s>>>(A);
+    else if (add) sweep_kernel<RT, MODE, false, true><<<grid, kBlock, 0, s>>>(A);
+    else sweep_kernel<RT, MODE, false, false><<<grid, kBlock, 0, s>>>(A);
 }
 
-int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const uint32_t* ptr, const uint32_t* idx, void* res,
-                 const float* a, const float* b, const float* c, const float* d, const float* y, float* out,
-                 float* save) {
+template <int RT>
+void launch_rt(const SweepArgs& A, int mode, bool sub, bool add, unsigned grid, cudaStream_t s) {
+    if (mode == M_CSC) launch_mode<RT, M_CSC>(A, sub, add, grid, s);
+    else if (mode == M_CSR) launch_mode<RT, M_CSR>(A, sub, add, grid, s);
+    else launch_mode<RT, M_PLAIN>(A, false, false, grid, s);
+}
+
+SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const uint32_t* idx, void* res) {
     SweepArgs A;
+    std::memset(&A, 0, sizeof(A));
     A.ptr = ptr;
     A.idx = idx;
     A.res = res;
-    A.a = a;
-    A.b = b;
-    A.c = c;
-    A.d = d;
-    A.y = y;
-    A.out = out;
-    A.save = save;
     A.lambda = h->o.lambda;
     A.xt = D.x;
     A.cl = D.c;
@@ -263,14 +278,18 @@ int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const uint32_t* ptr
     A.nwb = D.nwb;
     A.part = D.part;
     A.xcount = D.xcount;
+    return A;
+}
+
+int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A, int mode, bool sub, bool add) {
     const unsigned grid = D.nx + D.nc + D.nwb + D.ntb;
     if (grid == 0) return CDMF_OK;
     {
         Timed tm(h, kind);
         switch (h->rt) {
-            case 0: launch_sweep_rt<0>(A, a != nullptr, c != nullptr, grid, h->s); break;
-            case 1: launch_sweep_rt<1>(A, a != nullptr, c != nullptr, grid, h->s); break;
-            default: launch_sweep_rt<2>(A, a != nullptr, c != nullptr, grid, h->s); break;
+            case 0: launch_rt<0>(A, mode, sub, add, grid, h->s); break;
+            case 1: launch_rt<1>(A, mode, sub, add, grid, h->s); break;
+            default: launch_rt<2>(A, mode, sub, add, grid, h->s); break;
         }
     }
     CU(h, cudaGetLastError());
@@ -283,36 +302,64 @@ int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const uint32_t* ptr
 // One feature t of outer iteration `oiter`.
 int feature_step(cdmf_handle* h, uint32_t t, int oiter) {
     const int64_t m = h->m, n = h->n;
+    const uint32_t k = h->o.k;
     float* Wt = h->W + (size_t)t * m;
     float* Ht = h->H + (size_t)t * n;
     const int tp = h->pending;
-    const float* Wp = tp >= 0 ? h->W + (size_t)tp * m : nullptr;
-    const float* Hp = tp >= 0 ? h->H + (size_t)tp * n : nullptr;
-    const bool add = oiter > 1;
-    int r;
-    for (int it = 1; it <= h->o.maxinneriter; ++it) {
-        const bool first = it == 1;
-        // h_t over CSC: cross vectors are rows (length m)
-        r = launch_sweep(h, K_CSC, h->csc, h->csc_ptr, h->csc_idx, h->res_csc, first ? Wp : nullptr,
-                         first ? Hp : nullptr, first && add ? Wt : nullptr, first && add ? Ht : nullptr, Wt, Ht,
-                         first ? h->hsave : nullptr);
-        if (r) return r;
-        // w_t over CSR: cross vectors are columns (length n).  H[tp] was
-        // overwritten above when tp == t (k == 1); hsave holds its old value.
-        const float* Hp_csr = (tp == (int)t) ? h->hsave : Hp;
-        r = launch_sweep(h, K_CSR, h->csr, h->csr_ptr, h->csr_idx, h->res_csr, first ? Hp_csr : nullptr,
-                         first ? Wp : nullptr, first && add ? h->hsave : nullptr, first && add ? Wt : nullptr, Ht, Wt,
-                         nullptr);
-        if (r) return r;
+    const bool sub = tp >= 0, add = oiter > 1;
+    const float* Wp = sub ? h->W + (size_t)tp * m : nullptr;
+    const float* Hp = sub ? h->H + (size_t)tp * n : nullptr;
+    const float* Wnext = h->W + (size_t)((t + 1) % k) * m;
+    const int T = h->o.maxinneriter;
+    if (T <= 0) return CDMF_OK;
+    if (h->p_for != (int)t) {
+        if (m) {
+            pack_p_kernel<<<(unsigned)std::min<int64_t>(4096, (m + 255) / 256), 256, 0, h->s>>>(h->P, Wp, Wt, m);
+            CU(h, cudaGetLastError());
+            h->st.launches++;
+        }
+        h->p_for = (int)t;
     }
-    if (h->o.maxinneriter > 0) h->pending = (int)t;
+    int r;
+    for (int it = 1; it <= T; ++it) {
+        const bool first = it == 1, last = it == T;
+        // h_t over CSC: cross vectors are rows (length m)
+        SweepArgs A = base_args(h, h->csc, h->csc_ptr, h->csc_idx, h->res_csc);
+        A.out = Ht;
+        if (first) {
+            A.P = h->P;
+            A.b = Hp;
+            A.d = Ht;
+            A.emitQ = h->Q;
+        } else {
+            A.y = Wt;
+        }
+        if ((r = launch_sweep(h, K_CSC, h->csc, A, first ? M_CSC : M_PLAIN, sub, add))) return r;
+        // w_t over CSR: cross vectors are columns (length n)
+        SweepArgs B = base_args(h, h->csr, h->csr_ptr, h->csr_idx, h->res_csr);
+        B.out = Wt;
+        if (first) {
+            B.Q = h->Q;
+            B.b = Wp;
+            B.d = Wt;
+        } else {
+            B.y = Ht;
+        }
+        if (last) {
+            B.emitP = h->P;
+            B.next_old = Wnext;
+        }
+        if ((r = launch_sweep(h, K_CSR, h->csr, B, first ? M_CSR : M_PLAIN, sub, add))) return r;
+    }
+    h->p_for = (int)((t + 1) % k);
+    h->pending = (int)t;
     return CDMF_OK;
 }
 
 int launch_rmse(cdmf_handle* h, double* dst) {
     Timed tm(h, K_RMSE);
-    rmse_kernel<<<h->rmse_grid, kBlock, 0, h->s>>>(h->te_row, h->te_col, h->te_val, h->nt, h->W, h->H, h->m, h->n,
-                                                  h->o.k, h->rmse_part, h->rmse_count, dst);
+    rmse_kernel<float><<<h->rmse_grid, kBlock, 0, h->s>>>(h->te_row, h->te_col, h->te_val, h->nt, h->W, h->H, h->m,
+                                                         h->n, h->o.k, h->rmse_part, h->rmse_count, dst, nullptr);
     CU(h, cudaGetLastError());
     h->st.launches++;
     h->st.rmse_launches++;
@@ -342,6 +389,37 @@ int flush_pending(cdmf_handle* h) {
     }
     CU(h, cudaGetLastError());
     h->pending = -1;
+    h->p_for = -1;
+    return CDMF_OK;
+}
+
+// 16-bit modes: recompute both residual copies from the FP32 ratings and
+// factors (clears the pending subtract).
+int refresh_residual(cdmf_handle* h) {
+    const int tp = h->pending;
+    const float* pa = tp >= 0 ? h->H + (size_t)tp * h->n : nullptr;
+    const float* pb = tp >= 0 ? h->W + (size_t)tp * h->m : nullptr;
+    {
+        Timed tm(h, K_REFRESH);
+        dim3 gw((unsigned)((h->m + 31) / 32), (h->kp + 31) / 32), gh((unsigned)((h->n + 31) / 32), (h->kp + 31) / 32);
+        if (h->m) to_row_major_kernel<<<gw, kBlock, 0, h->s>>>(h->W, h->Wrm, h->o.k, h->kp, h->m);
+        if (h->n) to_row_major_kernel<<<gh, kBlock, 0, h->s>>>(h->H, h->Hrm, h->o.k, h->kp, h->n);
+        if (h->rt == 1)
+            refresh_kernel<1><<<h->ref_grid, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->csr_val, h->to_csc, h->m,
+                                                               h->nnz, h->Wrm, h->Hrm, h->kp, h->res_csr, h->res_csc,
+                                                               pa, pb, h->ref_part, h->ref_count, h->drift_out,
+                                                               h->nonfinite);
+        else
+            refresh_kernel<2><<<h->ref_grid, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->csr_val, h->to_csc, h->m,
+                                                               h->nnz, h->Wrm, h->Hrm, h->kp, h->res_csr, h->res_csc,
+                                                               pa, pb, h->ref_part, h->ref_count, h->drift_out,
+                                                               h->nonfinite);
+    }
+    CU(h, cudaGetLastError());
+    h->st.launches += 3;
+    h->st.refresh_launches += 1;
+    h->pending = -1;
+    h->refreshed = true;
     return CDMF_OK;
 }
 
@@ -434,7 +512,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         return CDMF_ERR_INVALID;
     if (o->residual < 0 || o->residual > 2 || o->reduce < 0 || o->reduce > 1 || o->version < 1 || o->version > 3)
         return CDMF_ERR_INVALID;
-    if (p->nnz > (int64_t)UINT32_MAX || p->m >= (int64_t)UINT32_MAX || p->n >= (int64_t)UINT32_MAX ||
+    if (p->nnz > (int64_t)UINT32_MAX - 8192 || p->m >= (int64_t)UINT32_MAX || p->n >= (int64_t)UINT32_MAX ||
         p->nnz_test > (int64_t)INT32_MAX * 64)
         return CDMF_ERR_TOO_LARGE;
     int r;
@@ -467,7 +545,8 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if ((r = dalloc(h, &h->csr_ptr, m + 1)) || (r = dalloc(h, &h->csr_idx, N)) || (r = dalloc(h, &h->csc_ptr, n + 1)) ||
         (r = dalloc(h, &h->csc_idx, N)) || (r = dalloc(h, &h->csr_val, N)) || (r = dalloc(h, &h->csc_val, N)) ||
         (r = dalloc(h, (char**)&h->res_csr, N * h->rbytes)) || (r = dalloc(h, (char**)&h->res_csc, N * h->rbytes)) ||
-        (r = dalloc(h, &h->W, k * m)) || (r = dalloc(h, &h->H, k * n)) || (r = dalloc(h, &h->hsave, n)) ||
+        (r = dalloc(h, &h->W, k * m)) || (r = dalloc(h, &h->H, k * n)) || (r = dalloc(h, &h->P, m)) ||
+        (r = dalloc(h, &h->Q, n)) ||
         (r = dalloc(h, &h->te_row, h->nt)) || (r = dalloc(h, &h->te_col, h->nt)) || (r = dalloc(h, &h->te_val, h->nt)))
         return bail(r);
     h->rmse_grid = (int)std::max<int64_t>(1, std::min<int64_t>(4 * 152, (h->nt + kBlock - 1) / kBlock));
@@ -487,6 +566,33 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         (r = up(h->te_val, p->test_val, 4 * h->nt)))
         return bail(r);
     if (cudaMemsetAsync(h->rmse_count, 0, 4, h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    if (h->rt != 0) {
+        // CSR position -> CSC position; also proves the CSC arrays are the
+        // transpose of the CSR arrays, which the refresh scatter relies on
+        std::vector<uint32_t> to_csc(N), next(p->csc_col_ptr, p->csc_col_ptr + n);
+        for (int64_t i = 0; i < m; ++i)
+            for (uint32_t q = p->csr_row_ptr[i]; q < p->csr_row_ptr[i + 1]; ++q) {
+                const uint32_t j = p->csr_col_idx[q];
+                const uint32_t pos = next[j]++;
+                if (pos >= p->csc_col_ptr[j + 1] || p->csc_row_idx[pos] != (uint32_t)i ||
+                    p->csc_val[pos] != p->csr_val[q])
+                    return bail(CDMF_ERR_INVALID);
+                to_csc[q] = pos;
+            }
+        h->kp = (o->k + 3) / 4 * 4;
+        const int64_t nchunks = (N + kRefreshChunk - 1) / kRefreshChunk;
+        h->ref_grid = (int)std::max<int64_t>(1, std::min<int64_t>(152 * 8, nchunks));
+        if ((r = dalloc(h, &h->to_csc, N)) || (r = dalloc(h, &h->Wrm, (size_t)m * h->kp)) ||
+            (r = dalloc(h, &h->Hrm, (size_t)n * h->kp)) || (r = dalloc(h, &h->ref_part, h->ref_grid)) ||
+            (r = dalloc(h, &h->drift_out, 1)) || (r = dalloc(h, &h->ref_count, 1)) || (r = dalloc(h, &h->nonfinite, 1)))
+            return bail(r);
+        if ((r = up(h->to_csc, to_csc.data(), 4 * N))) return bail(r);
+        if (cudaMemsetAsync(h->ref_count, 0, 4, h->s) != cudaSuccess ||
+            cudaMemsetAsync(h->nonfinite, 0, 8, h->s) != cudaSuccess ||
+            cudaMemsetAsync(h->drift_out, 0, 8, h->s) != cudaSuccess ||
+            cudaStreamSynchronize(h->s) != cudaSuccess)
+            return bail(CDMF_ERR_CUDA);
+    }
     const bool seq = o->reduce == CDMF_REDUCE_SEQUENTIAL;
     BinCfg cfg;
     if ((r = upload_bins(h, h->csr, plan_bins(p->csr_row_ptr, m, seq, cfg))) ||
@@ -517,6 +623,7 @@ int cdmf_cuda_set_factors(cdmf_handle* h, const float* W0, const float* H0) {
     int r;
     if ((r = reset_residual(h, h->res_csr, h->csr_val)) || (r = reset_residual(h, h->res_csc, h->csc_val))) return r;
     h->pending = -1;
+    h->p_for = -1;
     h->next_oiter = 1;
     CU(h, cudaStreamSynchronize(h->s));
     return CDMF_OK;
@@ -531,6 +638,10 @@ int cdmf_cuda_run(cdmf_handle* h, int n_outer, double* rmse_out) {
     h->st.launches = h->st.sweep_csc_launches = h->st.sweep_csr_launches = 0;
     h->st.rmse_launches = h->st.refresh_launches = 0;
     h->st.updates = 0;
+    h->st.drift_rms = 0;
+    h->st.nonfinite = 0;
+    h->refreshed = false;
+    if (h->rt != 0) CU(h, cudaMemsetAsync(h->nonfinite, 0, 8, h->s));
     h->marks.clear();
     h->pool_used = 0;
     std::vector<double> rm(std::max(1, n_outer), 0.0);
@@ -542,6 +653,10 @@ int cdmf_cuda_run(cdmf_handle* h, int n_outer, double* rmse_out) {
         const int chunk = std::min(n_outer - done, slots);
         for (int q = 0; q < chunk; ++q) {
             const int oiter = h->next_oiter;
+            if (h->rt != 0 && oiter > 1 && h->nnz > 0) {
+                int r = refresh_residual(h);
+                if (r) return r;
+            }
             for (uint32_t t = 0; t < h->o.k; ++t) {
                 int r = feature_step(h, t, oiter);
                 if (r) return r;
@@ -573,6 +688,15 @@ int cdmf_cuda_run(cdmf_handle* h, int n_outer, double* rmse_out) {
         else h->st.refresh_ms += t;
     }
     if (rmse_out) for (int q = 0; q < n_outer; ++q) rmse_out[q] = rm[q];
+    if (h->rt != 0 && h->refreshed) {
+        double drift = 0;
+        unsigned long long bad = 0;
+        CU(h, cudaMemcpy(&drift, h->drift_out, 8, cudaMemcpyDeviceToHost));
+        CU(h, cudaMemcpy(&bad, h->nonfinite, 8, cudaMemcpyDeviceToHost));
+        h->st.drift_rms = h->nnz ? std::sqrt(drift / (double)h->nnz) : 0.0;
+        h->st.nonfinite = (int64_t)bad;
+        if (bad) return fail(h, CDMF_ERR_NUMERIC, "non-finite residual values at the refresh");
+    }
     return CDMF_OK;
 }
 
@@ -647,6 +771,7 @@ int cdmf_cuda_set_state(cdmf_handle* h, const float* W, const float* H, const fl
     if ((r = upres(h->res_csc, res_csc)) || (r = upres(h->res_csr, res_csr))) return r;
     CU(h, cudaStreamSynchronize(h->s));
     h->pending = -1;
+    h->p_for = -1;
     h->next_oiter = next_oiter;
     return CDMF_OK;
 }
@@ -671,6 +796,54 @@ int cdmf_cuda_bins(const cdmf_handle* h, int which, int64_t counts[4], int64_t n
         if (nnz) nnz[q] = B.nnz[q];
     }
     return CDMF_OK;
+}
+
+int cdmf_cuda_rmse_coo(uint32_t k, int64_t m, int64_t n, const float* W, const float* H, int64_t nnz_test,
+                       const uint32_t* test_row, const uint32_t* test_col, const double* test_val, int device,
+                       double* rmse, int64_t* nan_count) {
+    if (k == 0 || m < 0 || n < 0 || nnz_test < 0 || !W || !H || !rmse) return CDMF_ERR_INVALID;
+    if (nnz_test == 0) return CDMF_ERR_EMPTY_TEST;
+    if (!test_row || !test_col || !test_val) return CDMF_ERR_INVALID;
+    for (int64_t e = 0; e < nnz_test; ++e)
+        if ((int64_t)test_row[e] >= m || (int64_t)test_col[e] >= n) return CDMF_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return CDMF_ERR_NO_DEVICE;
+    if (cudaSetDevice(device) != cudaSuccess) return CDMF_ERR_NO_DEVICE;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(4 * 152, (nnz_test + kBlock - 1) / kBlock));
+    const size_t wb = sizeof(float) * k * m, hb = sizeof(float) * k * n;
+    char* buf = nullptr;
+    // one block: W | H | rows | cols | vals | partials | out | nan count | counter
+    size_t off[9], tot = 0;
+    const size_t sz[9] = {wb, hb, 4 * (size_t)nnz_test, 4 * (size_t)nnz_test, 8 * (size_t)nnz_test,
+                          8 * (size_t)grid, 8, 8, 4};
+    for (int q = 0; q < 9; ++q) { off[q] = tot; tot += (sz[q] + 255) / 256 * 256; }
+    if (cudaMalloc((void**)&buf, tot) != cudaSuccess) return CDMF_ERR_ALLOC;
+    int st = CDMF_OK;
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) { cudaFree(buf); return CDMF_ERR_CUDA; }
+    unsigned long long nans = 0;
+    bool ok = cudaMemcpyAsync(buf + off[0], W, wb, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(buf + off[1], H, hb, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(buf + off[2], test_row, sz[2], cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(buf + off[3], test_col, sz[3], cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemcpyAsync(buf + off[4], test_val, sz[4], cudaMemcpyHostToDevice, s) == cudaSuccess &&
+              cudaMemsetAsync(buf + off[7], 0, 8, s) == cudaSuccess && cudaMemsetAsync(buf + off[8], 0, 4, s) == cudaSuccess;
+    if (ok) {
+        rmse_kernel<double><<<grid, kBlock, 0, s>>>((const uint32_t*)(buf + off[2]), (const uint32_t*)(buf + off[3]),
+                                                    (const double*)(buf + off[4]), nnz_test, (const float*)(buf + off[0]),
+                                                    (const float*)(buf + off[1]), m, n, k, (double*)(buf + off[5]),
+                                                    (uint32_t*)(buf + off[8]), (double*)(buf + off[6]),
+                                                    (unsigned long long*)(buf + off[7]));
+        ok = cudaGetLastError() == cudaSuccess &&
+             cudaMemcpyAsync(rmse, buf + off[6], 8, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+             cudaMemcpyAsync(&nans, buf + off[7], 8, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+             cudaStreamSynchronize(s) == cudaSuccess;
+    }
+    if (!ok) st = CDMF_ERR_CUDA;
+    if (nan_count) *nan_count = (int64_t)nans;
+    cudaStreamDestroy(s);
+    cudaFree(buf);
+    return st;
 }
 
 int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* H, double* rmse_out, cdmf_outer_cb cb,

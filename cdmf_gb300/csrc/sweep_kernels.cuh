@@ -14,6 +14,18 @@
 // x86-64 build, so a line summed by one thread in index order reproduces the
 // reference bit for bit.
 //
+// Gathers.  The per-nonzero cross-vector values (a_i, c_i, y_i) are read from
+// one packed table per sweep so each nonzero costs a single gather:
+//   CSC first sweep: P[i] = (W[t-1][i] new, W[t][i] old)         float2, = (a, c=y)
+//   CSR first sweep: Q[j] = (H[t-1][j] new, H[t][j] old, H[t][j] new, 0)  float4
+// The CSC sweep writes Q as it finishes each column; the last CSR sweep of a
+// feature writes P for the next feature as it finishes each row.
+//
+// Streams.  Inside a line, index and residual are read with 128-bit (16-bit
+// residual: 64-bit) vector loads, 4 nonzeros per lane per load, after a
+// scalar head that reaches a 4-element boundary; cache-streaming hints keep
+// them out of L1, which holds the gather tables.
+//
 // Lines are binned by length and all bins run in the same launch:
 //   blocks [0, nx)            one chunk of a split line (len > cta_max); the
 //                             last chunk to finish combines the chunk partials
@@ -31,6 +43,11 @@ namespace cdmf {
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 
+// sweep modes
+constexpr int M_PLAIN = 0;  // inner iterations >= 2: y only, no residual writes
+constexpr int M_CSC = 1;    // first CSC sweep of a feature: P gathers, emits Q
+constexpr int M_CSR = 2;    // first CSR sweep of a feature: Q gathers
+
 struct XTask {            // one chunk of a split line
     uint32_t line, beg, end, slot;
     uint32_t xl, first_slot, nchunks, pad;
@@ -40,13 +57,15 @@ struct SweepArgs {
     const uint32_t* __restrict__ ptr;
     const uint32_t* __restrict__ idx;
     void* __restrict__ res;
-    const float* __restrict__ a;   // subtract: cross vector (previous feature, final)
-    const float* b;                // subtract: line vector  (previous feature, final)
-    const float* __restrict__ c;   // add-back: cross vector (this feature, old)
-    const float* d;                // add-back: line vector  (this feature, old)
-    const float* __restrict__ y;   // solve: cross vector
+    const float* __restrict__ y;   // M_PLAIN: cross vector
+    const float2* __restrict__ P;  // M_CSC: packed cross table
+    const float4* __restrict__ Q;  // M_CSR: packed cross table
+    const float* b;                // subtract: line vector (previous feature, final)
+    const float* d;                // add-back: line vector (this feature, old)
     float* out;                    // solve: line vector (written)
-    float* save;                   // optional copy of out's old value
+    float4* emitQ;                 // M_CSC: Q[j] = (b_j, d_j, x_j, 0)
+    float2* emitP;                 // CSR sweeps that end a feature: P[i] = (x_i, next_old[i])
+    const float* next_old;         // W of the next feature (old), for emitP
     float lambda;
     // work lists
     const XTask* xt;
@@ -62,64 +81,171 @@ struct SweepArgs {
 // ---- residual element access -------------------------------------------------
 template <int RT> struct Res;
 template <> struct Res<0> {
-    using T = float;
     static __device__ __forceinline__ float ld(const void* p, uint32_t q) { return __ldcs((const float*)p + q); }
     static __device__ __forceinline__ float st(void* p, uint32_t q, float v) { __stcs((float*)p + q, v); return v; }
-};
-template <> struct Res<1> {
-    using T = __nv_bfloat16;
-    static __device__ __forceinline__ float ld(const void* p, uint32_t q) {
-        unsigned short u = __ldcs((const unsigned short*)p + q);
-        return __bfloat162float(__ushort_as_bfloat16(u));
+    static __device__ __forceinline__ void ld4(const void* p, uint32_t q, float (&r)[4]) {
+        const float4 v = __ldcs((const float4*)((const float*)p + q));
+        r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
     }
-    static __device__ __forceinline__ float st(void* p, uint32_t q, float v) {
-        __nv_bfloat16 h = __float2bfloat16_rn(v);
-        __stcs((unsigned short*)p + q, __bfloat16_as_ushort(h));
-        return __bfloat162float(h);
+    static __device__ __forceinline__ void st4(void* p, uint32_t q, float (&r)[4]) {
+        __stcs((float4*)((float*)p + q), make_float4(r[0], r[1], r[2], r[3]));
     }
 };
-template <> struct Res<2> {
-    using T = __half;
-    static __device__ __forceinline__ float ld(const void* p, uint32_t q) {
-        unsigned short u = __ldcs((const unsigned short*)p + q);
+template <int KIND> struct Res16 {
+    static __device__ __forceinline__ float to_f(unsigned short u) {
+        if (KIND == 1) return __bfloat162float(__ushort_as_bfloat16(u));
         return __half2float(__ushort_as_half(u));
     }
+    static __device__ __forceinline__ unsigned short from_f(float v, float& rounded) {
+        if (KIND == 1) {
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            rounded = __bfloat162float(h);
+            return __bfloat16_as_ushort(h);
+        }
+        const __half h = __float2half_rn(v);
+        rounded = __half2float(h);
+        return __half_as_ushort(h);
+    }
+    static __device__ __forceinline__ float ld(const void* p, uint32_t q) {
+        return to_f(__ldcs((const unsigned short*)p + q));
+    }
     static __device__ __forceinline__ float st(void* p, uint32_t q, float v) {
-        __half h = __float2half_rn(v);
-        __stcs((unsigned short*)p + q, __half_as_ushort(h));
-        return __half2float(h);
+        float rv;
+        __stcs((unsigned short*)p + q, from_f(v, rv));
+        return rv;
+    }
+    static __device__ __forceinline__ void ld4(const void* p, uint32_t q, float (&r)[4]) {
+        const uint2 v = __ldcs((const uint2*)((const unsigned short*)p + q));
+        r[0] = to_f((unsigned short)(v.x & 0xffff));
+        r[1] = to_f((unsigned short)(v.x >> 16));
+        r[2] = to_f((unsigned short)(v.y & 0xffff));
+        r[3] = to_f((unsigned short)(v.y >> 16));
+    }
+    // rounds r[] to storage precision in place and stores
+    static __device__ __forceinline__ void st4(void* p, uint32_t q, float (&r)[4]) {
+        const unsigned u0 = from_f(r[0], r[0]), u1 = from_f(r[1], r[1]), u2 = from_f(r[2], r[2]),
+                       u3 = from_f(r[3], r[3]);
+        __stcs((uint2*)((unsigned short*)p + q), make_uint2(u0 | (u1 << 16), u2 | (u3 << 16)));
     }
 };
+template <> struct Res<1> : Res16<1> {};
+template <> struct Res<2> : Res16<2> {};
 
-// One element: fused residual update + accumulation.
-template <int RT, bool SUB, bool ADD>
-__device__ __forceinline__ void elem(const SweepArgs& A, uint32_t q, float r, uint32_t i, float bj, float dj,
-                                     float& g, float& h) {
-    if (SUB) r = __fsub_rn(r, __fmul_rn(__ldg(A.a + i), bj));
-    if (ADD) r = __fadd_rn(r, __fmul_rn(__ldg(A.c + i), dj));
-    if (SUB || ADD) r = Res<RT>::st(A.res, q, r);
-    const float yi = __ldg(A.y + i);
-    g = __fadd_rn(g, __fmul_rn(yi, r));
-    h = __fadd_rn(h, __fmul_rn(yi, yi));
+// Running sum; with KAHAN the lost low-order part is carried in `c`
+// (compensated summation, used for lines longer than the warp bin when the
+// residual is stored in 16 bits).
+template <bool KAHAN> struct Acc {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        if (KAHAN) {
+            const float y = __fsub_rn(x, c);
+            const float t = __fadd_rn(s, y);
+            c = __fsub_rn(__fsub_rn(t, s), y);
+            s = t;
+        } else {
+            s = __fadd_rn(s, x);
+        }
+    }
+    __device__ __forceinline__ float value() const { return KAHAN ? __fsub_rn(s, c) : s; }
+};
+
+// Cross-vector values of one nonzero with cross index i.
+template <int MODE>
+__device__ __forceinline__ void fetch(const SweepArgs& A, uint32_t i, float& a, float& c, float& y) {
+    if (MODE == M_CSC) {
+        const float2 p = __ldg(A.P + i);
+        a = p.x;
+        c = p.y;
+        y = p.y;
+    } else if (MODE == M_CSR) {
+        const float4 q = __ldg(A.Q + i);
+        a = q.x;
+        c = q.y;
+        y = q.z;
+    } else {
+        a = c = 0.0f;
+        y = __ldg(A.y + i);
+    }
 }
 
-// Strided pass over [beg, end): this thread takes beg+lane, beg+lane+S, ...
-// in increasing order, four loads in flight per step.
-template <int RT, bool SUB, bool ADD, int S>
+template <bool SUB, bool ADD>
+__device__ __forceinline__ float update(float r, float a, float c, float bj, float dj) {
+    if (SUB) r = __fsub_rn(r, __fmul_rn(a, bj));
+    if (ADD) r = __fadd_rn(r, __fmul_rn(c, dj));
+    return r;
+}
+
+template <class AccT>
+__device__ __forceinline__ void accumulate(AccT& g, AccT& h, float y, float r) {
+    g.add(__fmul_rn(y, r));
+    h.add(__fmul_rn(y, y));
+}
+
+// One scalar element: update, store, accumulate.
+template <int RT, int MODE, bool SUB, bool ADD, class AccT>
+__device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, float dj, AccT& g, AccT& h) {
+    const uint32_t i = __ldcs(A.idx + q);
+    float r = Res<RT>::ld(A.res, q);
+    float a, c, y;
+    fetch<MODE>(A, i, a, c, y);
+    if (SUB || ADD) r = Res<RT>::st(A.res, q, update<SUB, ADD>(r, a, c, bj, dj));
+    accumulate(g, h, y, r);
+}
+
+// Pass over [beg, end) by S cooperating threads (this one is `lane`): a scalar
+// head up to the first 4-aligned position (lanes 0..2), then 4-element vector
+// chunks (chunk c to lane c mod S, two chunks in flight per lane), then a
+// scalar tail.  Each lane visits its elements in increasing order.
+template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
-                                        float dj, float& g, float& h) {
-    uint32_t q = beg + lane;
-    for (; q + 3 * S < end; q += 4 * S) {
-        uint32_t i0 = __ldcs(A.idx + q), i1 = __ldcs(A.idx + q + S), i2 = __ldcs(A.idx + q + 2 * S),
-                 i3 = __ldcs(A.idx + q + 3 * S);
-        float r0 = Res<RT>::ld(A.res, q), r1 = Res<RT>::ld(A.res, q + S), r2 = Res<RT>::ld(A.res, q + 2 * S),
-              r3 = Res<RT>::ld(A.res, q + 3 * S);
-        elem<RT, SUB, ADD>(A, q, r0, i0, bj, dj, g, h);
-        elem<RT, SUB, ADD>(A, q + S, r1, i1, bj, dj, g, h);
-        elem<RT, SUB, ADD>(A, q + 2 * S, r2, i2, bj, dj, g, h);
-        elem<RT, SUB, ADD>(A, q + 3 * S, r3, i3, bj, dj, g, h);
+                                        float dj, float& gs, float& hs) {
+    Acc<KAHAN> g, h;
+    uint32_t vbeg = (beg + 3u) & ~3u;
+    if (vbeg > end) vbeg = end;
+    const uint32_t vend = vbeg + ((end - vbeg) & ~3u);
+    if (lane < vbeg - beg) elem1<RT, MODE, SUB, ADD>(A, beg + lane, bj, dj, g, h);
+    uint32_t q = vbeg + 4u * lane;
+    for (; q + 4u * S < vend; q += 8u * S) {
+        uint32_t iv[2][4];
+        float r[2][4];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const uint4 v = __ldcs((const uint4*)(A.idx + q + 4u * S * u));
+            iv[u][0] = v.x; iv[u][1] = v.y; iv[u][2] = v.z; iv[u][3] = v.w;
+            Res<RT>::ld4(A.res, q + 4u * S * u, r[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            float y[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                float a, c;
+                fetch<MODE>(A, iv[u][e], a, c, y[e]);
+                r[u][e] = update<SUB, ADD>(r[u][e], a, c, bj, dj);
+            }
+            if (SUB || ADD) Res<RT>::st4(A.res, q + 4u * S * u, r[u]);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) accumulate(g, h, y[e], r[u][e]);
+        }
     }
-    for (; q < end; q += S) elem<RT, SUB, ADD>(A, q, Res<RT>::ld(A.res, q), __ldcs(A.idx + q), bj, dj, g, h);
+    if (q < vend) {
+        const uint4 v = __ldcs((const uint4*)(A.idx + q));
+        const uint32_t iv[4] = {v.x, v.y, v.z, v.w};
+        float r[4], y[4];
+        Res<RT>::ld4(A.res, q, r);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            float a, c;
+            fetch<MODE>(A, iv[e], a, c, y[e]);
+            r[e] = update<SUB, ADD>(r[e], a, c, bj, dj);
+        }
+        if (SUB || ADD) Res<RT>::st4(A.res, q, r);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) accumulate(g, h, y[e], r[e]);
+    }
+    if (lane < end - vend) elem1<RT, MODE, SUB, ADD>(A, vend + lane, bj, dj, g, h);
+    gs = g.value();
+    hs = h.value();
 }
 
 __device__ __forceinline__ void warp_sum2(float& g, float& h) {
@@ -146,22 +272,39 @@ __device__ __forceinline__ void cta_sum2(float& g, float& h) {
     }
 }
 
-// x_j from the accumulated sums; h excludes lambda * nnz_j.
-__device__ __forceinline__ void finish_line(const SweepArgs& A, uint32_t j, uint32_t len, float g, float h) {
-    const float lam = __fmul_rn(A.lambda, __uint2float_rn(len));
-    const float x = len == 0 ? 0.0f : __fdiv_rn(g, __fadd_rn(lam, h));
-    if (A.save) A.save[j] = A.out[j];
+// Writes x_j and the packed table entries derived from it.
+template <int MODE>
+__device__ __forceinline__ void write_line(const SweepArgs& A, uint32_t j, float x, float bj, float dj) {
     A.out[j] = x;
+    if (MODE == M_CSC) A.emitQ[j] = make_float4(bj, dj, x, 0.0f);
+    if (A.emitP) A.emitP[j] = make_float2(x, A.next_old == A.out ? x : A.next_old[j]);
 }
 
-template <int RT, bool SUB, bool ADD>
+// x_j from tree sums; h excludes lambda * nnz_j.
+template <int MODE>
+__device__ __forceinline__ void finish_line(const SweepArgs& A, uint32_t j, uint32_t len, float g, float h, float bj,
+                                            float dj) {
+    const float lam = __fmul_rn(A.lambda, __uint2float_rn(len));
+    write_line<MODE>(A, j, len == 0 ? 0.0f : __fdiv_rn(g, __fadd_rn(lam, h)), bj, dj);
+}
+
+// Per-line scalars: b_j (previous feature's final value) and d_j (this
+// feature's old value).  The CSC sweep also forwards them into Q.
+template <int MODE, bool SUB, bool ADD>
+__device__ __forceinline__ void line_scalars(const SweepArgs& A, uint32_t j, float& bj, float& dj) {
+    bj = (SUB || MODE == M_CSC) && A.b ? A.b[j] : 0.0f;
+    dj = (ADD || MODE == M_CSC) ? A.d[j] : 0.0f;
+}
+
+template <int RT, int MODE, bool SUB, bool ADD>
 __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepArgs A) {
     uint32_t b = blockIdx.x;
     if (b < A.nx) {                                        // split-line chunk
         const XTask T = A.xt[b];
-        const float bj = SUB ? A.b[T.line] : 0.0f, dj = ADD ? A.d[T.line] : 0.0f;
+        float bj, dj;
+        line_scalars<MODE, SUB, ADD>(A, T.line, bj, dj);
         float g = 0.0f, h = 0.0f;
-        strided<RT, SUB, ADD, kBlock>(A, T.beg, T.end, threadIdx.x, bj, dj, g, h);
+        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, T.beg, T.end, threadIdx.x, bj, dj, g, h);
         cta_sum2(g, h);
         __shared__ int last;
         if (threadIdx.x == 0) {
@@ -180,7 +323,7 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepArgs A) {
                 Hs = __fadd_rn(Hs, p.y);
             }
             const uint32_t len = A.ptr[T.line + 1] - A.ptr[T.line];
-            finish_line(A, T.line, len, G, Hs);
+            finish_line<MODE>(A, T.line, len, G, Hs, bj, dj);
             A.xcount[T.xl] = 0;
         }
         return;
@@ -189,11 +332,12 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepArgs A) {
     if (b < A.nc) {                                        // one line per CTA
         const uint32_t j = A.cl[b];
         const uint32_t beg = A.ptr[j], end = A.ptr[j + 1];
-        const float bj = SUB ? A.b[j] : 0.0f, dj = ADD ? A.d[j] : 0.0f;
+        float bj, dj;
+        line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
         float g = 0.0f, h = 0.0f;
-        strided<RT, SUB, ADD, kBlock>(A, beg, end, threadIdx.x, bj, dj, g, h);
+        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, beg, end, threadIdx.x, bj, dj, g, h);
         cta_sum2(g, h);
-        if (threadIdx.x == 0) finish_line(A, j, end - beg, g, h);
+        if (threadIdx.x == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
         return;
     }
     b -= A.nc;
@@ -203,11 +347,12 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepArgs A) {
         const uint32_t lane = threadIdx.x & 31;
         const uint32_t j = A.wl[w];
         const uint32_t beg = A.ptr[j], end = A.ptr[j + 1];
-        const float bj = SUB ? A.b[j] : 0.0f, dj = ADD ? A.d[j] : 0.0f;
+        float bj, dj;
+        line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
         float g = 0.0f, h = 0.0f;
-        strided<RT, SUB, ADD, 32>(A, beg, end, lane, bj, dj, g, h);
+        strided<RT, MODE, SUB, ADD, 32, false>(A, beg, end, lane, bj, dj, g, h);
         warp_sum2(g, h);
-        if (lane == 0) finish_line(A, j, end - beg, g, h);
+        if (lane == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
         return;
     }
     b -= A.nwb;
@@ -216,18 +361,24 @@ __global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepArgs A) {
     const uint32_t j = A.tl[t];
     const uint32_t beg = A.ptr[j], end = A.ptr[j + 1];
     const uint32_t len = end - beg;
+    float bj, dj;
+    line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
     if (len == 0) {
-        if (A.save) A.save[j] = A.out[j];
-        A.out[j] = 0.0f;
+        write_line<MODE>(A, j, 0.0f, bj, dj);
         return;
     }
-    const float bj = SUB ? A.b[j] : 0.0f, dj = ADD ? A.d[j] : 0.0f;
-    float g = 0.0f;
-    float h = __fmul_rn(A.lambda, __uint2float_rn(len));   // h starts at lambda*nnz (src/cdmf_ref.cpp:8)
-    for (uint32_t q = beg; q < end; ++q)
-        elem<RT, SUB, ADD>(A, q, Res<RT>::ld(A.res, q), __ldcs(A.idx + q), bj, dj, g, h);
-    if (A.save) A.save[j] = A.out[j];
-    A.out[j] = __fdiv_rn(g, h);
+    Acc<false> g, h;
+    h.s = __fmul_rn(A.lambda, __uint2float_rn(len));         // h starts at lambda*nnz (src/cdmf_ref.cpp:8)
+    for (uint32_t q = beg; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
+    write_line<MODE>(A, j, __fdiv_rn(g.s, h.s), bj, dj);
+}
+
+// P[i] = (prev[i] or 0, cur[i]): the packed CSC table when no sweep has
+// written it (start of a run, after a state change).
+__global__ void pack_p_kernel(float2* __restrict__ P, const float* __restrict__ prev, const float* __restrict__ cur,
+                              int64_t len) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
+        P[i] = make_float2(prev ? prev[i] : 0.0f, cur[i]);
 }
 
 // Applies a pending subtract r -= a_i * b_j to one residual copy (warp per
@@ -247,16 +398,20 @@ __global__ void __launch_bounds__(kBlock) flush_kernel(const uint32_t* __restric
     }
 }
 
-// Test RMSE (src/tools.cpp:543-582): per entry the float products
-// W[t][i]*H[t][j] are summed in double in t order, (pred - v)^2 in double, NaN
-// terms skipped but counted.  Fixed grid; block partials in double; the last
-// block adds them in block order and writes sqrt(sum / nnz_test).
+// Test RMSE (src/tools.cpp:543-582, and :489-541 for the text test file):
+// per entry the float products W[t][i]*H[t][j] are summed in double in t
+// order, (pred - v)^2 in double, NaN terms skipped but counted.  Fixed grid;
+// block partials in double; the last block adds them in block order and
+// writes sqrt(sum / nnz_test) and the NaN count.
+template <class VT>
 __global__ void __launch_bounds__(kBlock) rmse_kernel(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
-                                                      const float* __restrict__ val, int64_t nt,
+                                                      const VT* __restrict__ val, int64_t nt,
                                                       const float* __restrict__ W, const float* __restrict__ H,
                                                       int64_t m, int64_t n, uint32_t k, double* part,
-                                                      uint32_t* counter, double* out) {
+                                                      uint32_t* counter, double* out,
+                                                      unsigned long long* nan_out) {
     double acc = 0.0;
+    unsigned nans = 0;
     for (int64_t e = (int64_t)blockIdx.x * kBlock + threadIdx.x; e < nt; e += (int64_t)gridDim.x * kBlock) {
         const uint32_t i = row[e], j = col[e];
         double pred = 0.0;
@@ -265,17 +420,27 @@ __global__ void __launch_bounds__(kBlock) rmse_kernel(const uint32_t* __restrict
         const double dv = __dsub_rn(pred, (double)val[e]);
         const double tmp = __dmul_rn(dv, dv);
         if (!isnan(tmp)) acc = __dadd_rn(acc, tmp);
+        else nans++;
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc = __dadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+    for (int o = 16; o > 0; o >>= 1) {
+        acc = __dadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+        nans += __shfl_xor_sync(0xffffffffu, nans, o);
+    }
     __shared__ double sm[kWarps];
+    __shared__ unsigned smn[kWarps];
     __shared__ int last;
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    if ((threadIdx.x & 31) == 0) {
+        sm[threadIdx.x >> 5] = acc;
+        smn[threadIdx.x >> 5] = nans;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = sm[0];
-        for (int q = 1; q < kWarps; ++q) s = __dadd_rn(s, sm[q]);
+        unsigned long long c = smn[0];
+        for (int q = 1; q < kWarps; ++q) { s = __dadd_rn(s, sm[q]); c += smn[q]; }
         part[blockIdx.x] = s;
+        if (nan_out && c) atomicAdd(nan_out, c);
         __threadfence();
         last = (atomicAdd(counter, 1u) == gridDim.x - 1);
     }

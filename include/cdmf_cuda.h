@@ -99,7 +99,9 @@ typedef struct {
     int64_t launches;         /* kernels launched by the run */
     int64_t sweep_csc_launches, sweep_csr_launches, rmse_launches, refresh_launches;
     int64_t updates;          /* rank-one updates performed (outer iterations x k) */
-    double bytes_per_update;  /* compulsory HBM bytes of one rank-one update (see DESIGN) */
+    double bytes_per_update;  /* compulsory HBM bytes of one rank-one update */
+    double drift_rms;         /* 16-bit modes: RMS of (exact - stored) residual at the last refresh, FP64 */
+    int64_t nonfinite;        /* 16-bit modes: non-finite residuals found at the last refresh */
 } cdmf_stats;
 
 typedef struct cdmf_handle cdmf_handle;
@@ -116,6 +118,16 @@ int cdmf_cuda_version(void);
  * rmse_out (nullable) receives maxiter values when opts->rmse_each_outer. */
 int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* H,
                     double* rmse_out, cdmf_outer_cb cb, void* user);
+
+/* Test RMSE of given factors over a test COO with double values: the
+ * reference's calculate_rmse of the text test file (src/tools.cpp:489-541,
+ * values parsed with %lf, indices already 0-based).  Host pointers; the
+ * prediction and reduction run on `device`.  nan_count (nullable) receives
+ * the number of NaN terms, which are skipped in the sum but counted in the
+ * mean, as the reference does. */
+int cdmf_cuda_rmse_coo(uint32_t k, int64_t m, int64_t n, const float* W, const float* H, int64_t nnz_test,
+                       const uint32_t* test_row, const uint32_t* test_col, const double* test_val, int device,
+                       double* rmse, int64_t* nan_count);
 
 /* Handle API: the same engine split into upload / run / read-back. */
 int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** out);

@@ -4,13 +4,19 @@ Two reduction modes:
   sequential -- every line is summed by one thread in index order, the
                 reference's order: results must be BIT-EXACT after every outer
                 iteration (W, H, both residual copies) and the RMSE equal;
-  tree       -- the production mode (warp / CTA / split-line trees):
-                W and H within a relative 1e-5 of the reference after each
-                outer iteration, test RMSE within 1e-5 absolute.
-Relative error of x against x_ref: |x - x_ref| <= 1e-5 * max(|x_ref|, 0.1 * rms(x_ref_t))
-elementwise, where rms(x_ref_t) is the RMS of that feature's vector (the
-floor keeps entries that cancel to near zero from demanding more than FP32
-summation can give).
+  tree       -- the production mode (warp / CTA / split-line trees).  A
+                reordered FP32 sum cannot reproduce the reference's rounding,
+                and CCD++ amplifies rounding through the residual chain (the
+                first feature agrees to ~1e-7; later features inherit the
+                previous features' rounding), so the bar is the reference's
+                OWN FP32 error, measured against the FP64 oracle on the same
+                inputs.  After every outer iteration:
+                  fro(gpu - ref32) <= 2 * fro(ref32 - ref64) + 1e-6
+                  fro(gpu - ref64) <= 1.5 * fro(ref32 - ref64) + 1e-7
+                  elementwise rel(gpu, ref32) <= 2 * rel(ref32, ref64) + 1e-5
+                  |rmse_gpu - rmse_ref32| <= 1e-5
+                fro(x - r) = ||x - r||_F / ||r||_F; rel(x, r) = max |x - r| /
+                max(|r|, 0.1 * rms of r's feature vector).
 """
 import json
 import os
@@ -32,13 +38,29 @@ def bits(a):
     return np.ascontiguousarray(a).view(np.uint32)
 
 
-def rel_ok(x, ref, rtol=RTOL):
+def rel_err(x, ref):
     x = np.asarray(x, np.float64).reshape(ref.shape[0], -1)
     ref = np.asarray(ref, np.float64).reshape(ref.shape[0], -1)
     rms = np.sqrt(np.mean(ref * ref, axis=1, keepdims=True))
     scale = np.maximum(np.abs(ref), 0.1 * rms)
-    err = np.abs(x - ref) / np.where(scale > 0, scale, 1.0)
-    return float(err.max()) <= rtol, float(err.max())
+    return float((np.abs(x - ref) / np.where(scale > 0, scale, 1.0)).max())
+
+
+def fro(x, ref):
+    x = np.asarray(x, np.float64)
+    ref = np.asarray(ref, np.float64)
+    nr = np.linalg.norm(ref)
+    return float(np.linalg.norm(x - ref) / (nr if nr > 0 else 1.0))
+
+
+def within_budget(x, ref32, ref64):
+    """x (GPU, tree order) against the reference's own FP32 error budget."""
+    b_fro = fro(ref32, ref64)
+    b_rel = rel_err(ref32, ref64)
+    got = dict(fro32=fro(x, ref32), fro64=fro(x, ref64), rel32=rel_err(x, ref32), budget_fro=b_fro, budget_rel=b_rel)
+    ok = (got["fro32"] <= 2 * b_fro + 1e-6 and got["fro64"] <= 1.5 * b_fro + 1e-7
+          and got["rel32"] <= 2 * b_rel + 1e-5)
+    return ok, got
 
 
 @pytest.mark.parametrize("name", ["simple", "tricky_simple", "mini"])
@@ -59,17 +81,19 @@ def test_sequential_bit_exact_each_outer(name):
 
 
 @pytest.mark.parametrize("name", ["simple", "tricky_simple", "mini"])
-def test_tree_within_tolerance_each_outer(name):
+def test_tree_within_fp32_budget_each_outer(name):
     R, z = load_golden(name)
     md = META[name]
+    r64 = oracle.ccdpp(R, z["W0"].astype(np.float64), md["k"], md["lam"], md["maxiter"], md["maxinner"],
+                       dtype=np.float64, history=True)
     with engine.Engine(R, md["k"], md["lam"], md["maxiter"], md["maxinner"]) as e:
         e.set_factors(z["W0"])
         for j in range(md["maxiter"]):
             rm = e.run(1)
             W, H = e.factors()
-            okw, ew = rel_ok(W, z["W_hist"][j])
-            okh, eh = rel_ok(H, z["H_hist"][j])
-            assert okw and okh, (j, ew, eh)
+            okw, gw = within_budget(W, z["W_hist"][j], r64["W_hist"][j])
+            okh, gh = within_budget(H, z["H_hist"][j], r64["H_hist"][j])
+            assert okw and okh, (j, gw, gh)
             assert abs(rm[0] - z["rmse"][j]) <= RMSE_ATOL
 
 
@@ -87,6 +111,8 @@ def cpu_scale():
     W0 = synth.initial_w(run["k"], R.m, seed=0)
     ref = oracle.ccdpp(R, W0, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"], threads=8,
                        history=True, residuals=True)
+    ref["f64"] = oracle.ccdpp(R, W0.astype(np.float64), run["k"], run["lambda_"], run["maxiter"],
+                              run["maxinneriter"], threads=8, dtype=np.float64, history=True)
     return R, run, W0, ref
 
 
@@ -106,7 +132,7 @@ def test_cpu_scale_sequential_bit_exact(cpu_scale):
 
 def test_cpu_scale_tree_one_step_parity(cpu_scale):
     """From the oracle's state after outer j, one GPU outer iteration lands
-    within tolerance of the oracle's outer j+1 (errors do not compound)."""
+    within the FP32 budget of the oracle's outer j+1 (errors do not compound)."""
     R, run, W0, ref = cpu_scale
     k, lam, T = run["k"], run["lambda_"], run["maxinneriter"]
     W = W0.copy()
@@ -117,10 +143,13 @@ def test_cpu_scale_tree_one_step_parity(cpu_scale):
             e.set_state(W, H, rc, rr, j)
             rm = e.run(1)
             Wg, Hg = e.factors()
+            W64, H64 = W.astype(np.float64), H.astype(np.float64)
+            rc64, rr64 = rc.astype(np.float64), rr.astype(np.float64)
+            oracle.outer_iteration(R, W64, H64, rc64, rr64, k, lam, T, j, threads=8)
             oracle.outer_iteration(R, W, H, rc, rr, k, lam, T, j, threads=8)
-            okw, ew = rel_ok(Wg, W)
-            okh, eh = rel_ok(Hg, H)
-            assert okw and okh, (j, ew, eh)
+            okw, gw = within_budget(Wg, W, W64)
+            okh, gh = within_budget(Hg, H, H64)
+            assert okw and okh, (j, gw, gh)
             assert abs(rm[0] - oracle.rmse(R, W, H, k)) <= RMSE_ATOL
 
 
@@ -131,9 +160,9 @@ def test_cpu_scale_tree_free_running(cpu_scale):
         rm = e.run(run["maxiter"])
         W, H = e.factors()
     assert np.max(np.abs(rm - ref["rmse"])) <= RMSE_ATOL, (rm, ref["rmse"])
-    okw, ew = rel_ok(W, ref["W"], rtol=1e-4)
-    okh, eh = rel_ok(H, ref["H"], rtol=1e-4)
-    assert okw and okh, (ew, eh)
+    okw, gw = within_budget(W, ref["W"], ref["f64"]["W"])
+    okh, gh = within_budget(H, ref["H"], ref["f64"]["H"])
+    assert okw and okh, (gw, gh)
 
 
 @pytest.mark.parametrize("k,T", [(1, 3), (3, 1), (2, 2)])
@@ -164,19 +193,26 @@ def test_state_roundtrip_continues_identically():
     assert np.array_equal(bits(W), bits(z["W_hist"][3])) and np.array_equal(bits(H), bits(z["H_hist"][3]))
 
 
-def test_split_lines_bit_exact_in_sequential_and_close_in_tree():
+def test_split_lines_within_fp32_budget():
     # a matrix with very long columns exercises the split-line bin (> 16384 nnz)
     R = synth.generate(m=60000, n=40, nnz_total=900000, test_fraction=0.01, row_alpha=0.5, row_min=1, row_max=40,
                        col_alpha=0.3, col_cap=60000, rank=4, seed=21)
     W0 = synth.initial_w(4, R.m, seed=1)
     ref = oracle.ccdpp(R, W0, 4, 0.05, 2, 2, threads=8, history=True)
+    r64 = oracle.ccdpp(R, W0.astype(np.float64), 4, 0.05, 2, 2, threads=8, dtype=np.float64, history=True)
     with engine.Engine(R, 4, 0.05, 2, 2) as e:
         c, _ = e.bins("csc")
         assert c[3] > 0, c
         e.set_factors(W0)
-        rm = e.run(1)
+        for j in range(2):
+            rm = e.run(1)
+            W, H = e.factors()
+            okw, gw = within_budget(W, ref["W_hist"][j], r64["W_hist"][j])
+            okh, gh = within_budget(H, ref["H_hist"][j], r64["H_hist"][j])
+            assert okw and okh, (j, gw, gh)
+            assert abs(rm[0] - ref["rmse"][j]) <= RMSE_ATOL
+    with engine.Engine(R, 4, 0.05, 2, 2, reduce="sequential") as e:
+        e.set_factors(W0)
+        e.run(2)
         W, H = e.factors()
-    okw, ew = rel_ok(W, ref["W_hist"][0])
-    okh, eh = rel_ok(H, ref["H_hist"][0])
-    assert okw and okh, (ew, eh)
-    assert abs(rm[0] - ref["rmse"][0]) <= RMSE_ATOL
+    assert np.array_equal(bits(W), bits(ref["W"])) and np.array_equal(bits(H), bits(ref["H"]))
