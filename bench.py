@@ -168,6 +168,9 @@ def main():
     ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
     ap.add_argument("--residual", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--k", type=int, default=64)
+    ap.add_argument("--version", type=int, default=3, choices=[1, 2, 3],
+                    help="1/2: row-length-binned sweeps, 3: nonzero-balanced tiles")
+    ap.add_argument("--graph", type=int, default=1, help="replay outer iterations from CUDA graphs")
     ap.add_argument("--e2e-outer", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -219,7 +222,7 @@ def main():
     W0 = synth.initial_w(k, R.m, seed=rank)
 
     e = engine.Engine(R, k, lam, maxiter=max(args.steps, args.e2e_outer), maxinneriter=T, residual=args.residual,
-                      device=device)
+                      device=device, version=args.version, use_graph=bool(args.graph))
     e.set_factors(W0)
     e.run(args.warmup)
     # timed: device-resident
@@ -272,7 +275,8 @@ def main():
         "data": "synthetic (seeded, Netflix-shaped; the data set itself is not available)",
         "config": {"workload": f"{WORKLOAD} {R.m}x{R.n} train_nnz={R.nnz} test_nnz={R.nnz_test} k={k} "
                                f"lambda={lam} T={T}",
-                   "residual": args.residual, "step": "one outer iteration (k rank-one updates + test RMSE)",
+                   "residual": args.residual, "version": args.version, "cuda_graph": bool(args.graph),
+                   "step": "one outer iteration (k rank-one updates + test RMSE)",
                    "l2": "no flush: the residual copies streamed every feature exceed L2",
                    "parallelism": f"replicas x{ws}"},
         "outer_per_s": 1e3 * args.steps / t_ms,
@@ -282,7 +286,7 @@ def main():
         "clocks": clocks,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "sweep_kernel (CSC h-sweep + CSR w-sweep)",
+                     "kernel": ("tile_sweep_kernel" if args.version == 3 else "sweep_kernel") + " (CSC h-sweep + CSR w-sweep)",
                      "bytes_per_launch": bytes_launch, "mean_launch_ms": mean_launch_s * 1e3},
         "e2e": e2e,
         "cpu_baseline": cpu,
@@ -308,11 +312,12 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
     h2d = sum(getattr(Rp, f).nbytes for f in arrays) + W0.nbytes
     d2h = W0.nbytes + 4 * k * R.n + 8 * args.e2e_outer
     Wp[...] = W0
-    engine.train(Rp, Wp, k, lam, 1, T, residual=args.residual, device=device)  # warm the context
+    kw = dict(residual=args.residual, device=device, version=args.version, use_graph=bool(args.graph))
+    engine.train(Rp, Wp, k, lam, 1, T, **kw)  # warm the context
     dist.barrier()
     t0 = time.perf_counter()
     Wp[...] = W0
-    _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, residual=args.residual, device=device)
+    _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, **kw)
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_value = ws * k * args.e2e_outer / e2e_s
     return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

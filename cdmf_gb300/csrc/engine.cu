@@ -20,6 +20,7 @@
 #include "../../include/cdmf_cuda.h"
 #include "sweep_kernels.cuh"
 #include "refresh_kernels.cuh"
+#include "tile_kernels.cuh"
 
 #include <cuda_runtime.h>
 
@@ -39,6 +40,15 @@ struct Bins {
     std::vector<uint32_t> c, w, t;
     uint32_t nslots = 0, nxl = 0;
     int64_t count[4] = {0, 0, 0, 0}, nnz[4] = {0, 0, 0, 0};
+};
+
+// nonzero-balanced tiles of one compressed copy (version 3)
+struct DevTiles {
+    uint32_t* tile_line = nullptr;
+    float2 *head = nullptr, *tail = nullptr;
+    uint32_t* lcount = nullptr;
+    uint32_t* empty = nullptr;
+    uint32_t ntiles = 0, nempty = 0, tile_blocks = 0, empty_blocks = 0;
 };
 
 struct DevBins {
@@ -126,6 +136,8 @@ struct cdmf_handle {
     uint32_t* rmse_count = nullptr;
     int rmse_grid = 0;
     DevBins csr, csc;
+    DevTiles tcsr, tcsc;
+    bool tiles = false;              // version 3: nonzero-balanced tile sweeps
     // 16-bit residual modes: CSR->CSC position map, row-major factor copies
     uint32_t* to_csc = nullptr;
     float *Wrm = nullptr, *Hrm = nullptr;
@@ -135,6 +147,15 @@ struct cdmf_handle {
     uint32_t* ref_count = nullptr;
     unsigned long long* nonfinite = nullptr;
     bool refreshed = false;
+    // CUDA graphs of whole outer iterations, keyed by the schedule's signature
+    struct Graph {
+        int sig[5];
+        cudaGraphExec_t exec;
+        int end_pending, end_p_for;
+        int64_t launches, csc, csr, rmse, refresh;
+    };
+    std::vector<Graph> graphs;
+    double* rmse_graph_slot = nullptr;
     // state
     int next_oiter = 1;
     int pending = -1;                // feature whose subtract is still owed, -1 = none
@@ -212,6 +233,34 @@ int upload_bins(cdmf_handle* h, DevBins& D, Bins&& B) {
     return CDMF_OK;
 }
 
+int upload_tiles(cdmf_handle* h, DevTiles& D, const uint32_t* ptr, int64_t lines, int64_t nnz) {
+    std::vector<uint32_t> tl, empty;
+    const int64_t ntiles = (nnz + kWarpTile - 1) / kWarpTile;
+    tl.reserve(ntiles + 1);
+    int64_t L = 0;
+    for (int64_t t = 0; t < ntiles; ++t) {
+        const int64_t p = t * (int64_t)kWarpTile;
+        while (L < lines && (int64_t)ptr[L + 1] <= p) ++L;
+        tl.push_back((uint32_t)L);
+    }
+    tl.push_back((uint32_t)lines);
+    for (int64_t j = 0; j < lines; ++j)
+        if (ptr[j + 1] == ptr[j]) empty.push_back((uint32_t)j);
+    D.ntiles = (uint32_t)ntiles;
+    D.nempty = (uint32_t)empty.size();
+    D.tile_blocks = (D.ntiles + kWarps - 1) / kWarps;
+    D.empty_blocks = (D.nempty + kBlock - 1) / kBlock;
+    int r;
+    if ((r = dalloc(h, &D.tile_line, tl.size())) || (r = dalloc(h, &D.head, ntiles)) ||
+        (r = dalloc(h, &D.tail, ntiles)) || (r = dalloc(h, &D.lcount, lines)) || (r = dalloc(h, &D.empty, empty.size())))
+        return r;
+    CU(h, cudaMemcpyAsync(D.tile_line, tl.data(), 4 * tl.size(), cudaMemcpyHostToDevice, h->s));
+    if (!empty.empty()) CU(h, cudaMemcpyAsync(D.empty, empty.data(), 4 * empty.size(), cudaMemcpyHostToDevice, h->s));
+    CU(h, cudaMemsetAsync(D.lcount, 0, 4 * std::max<int64_t>(1, lines), h->s));
+    CU(h, cudaStreamSynchronize(h->s));
+    return CDMF_OK;
+}
+
 cudaEvent_t pool_event(cdmf_handle* h) {
     if (h->pool_used == h->pool.size()) {
         cudaEvent_t e;
@@ -260,6 +309,22 @@ void launch_rt(const SweepArgs& A, int mode, bool sub, bool add, unsigned grid, 
     else launch_mode<RT, M_PLAIN>(A, false, false, grid, s);
 }
 
+template <int RT, int MODE>
+void tile_mode(const TileArgs& T, bool sub, bool add, unsigned grid, cudaStream_t s) {
+    if (MODE == M_PLAIN) tile_sweep_kernel<RT, M_PLAIN, false, false><<<grid, kBlock, 0, s>>>(T);
+    else if (sub && add) tile_sweep_kernel<RT, MODE, true, true><<<grid, kBlock, 0, s>>>(T);
+    else if (sub) tile_sweep_kernel<RT, MODE, true, false><<<grid, kBlock, 0, s>>>(T);
+    else if (add) tile_sweep_kernel<RT, MODE, false, true><<<grid, kBlock, 0, s>>>(T);
+    else tile_sweep_kernel<RT, MODE, false, false><<<grid, kBlock, 0, s>>>(T);
+}
+
+template <int RT>
+void tile_rt(const TileArgs& T, int mode, bool sub, bool add, unsigned grid, cudaStream_t s) {
+    if (mode == M_CSC) tile_mode<RT, M_CSC>(T, sub, add, grid, s);
+    else if (mode == M_CSR) tile_mode<RT, M_CSR>(T, sub, add, grid, s);
+    else tile_mode<RT, M_PLAIN>(T, false, false, grid, s);
+}
+
 SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const uint32_t* idx, void* res) {
     SweepArgs A;
     std::memset(&A, 0, sizeof(A));
@@ -282,6 +347,35 @@ SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const
 }
 
 int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A, int mode, bool sub, bool add) {
+    if (h->tiles) {
+        const DevTiles& D3 = kind == K_CSC ? h->tcsc : h->tcsr;
+        TileArgs T;
+        T.s = A;
+        T.tile_line = D3.tile_line;
+        T.head = D3.head;
+        T.tail = D3.tail;
+        T.lcount = D3.lcount;
+        T.empty = D3.empty;
+        T.nempty = D3.nempty;
+        T.ntiles = D3.ntiles;
+        T.tile_blocks = D3.tile_blocks;
+        T.nnz = (uint32_t)h->nnz;
+        const unsigned grid = D3.tile_blocks + D3.empty_blocks;
+        if (grid == 0) return CDMF_OK;
+        {
+            Timed tm(h, kind);
+            switch (h->rt) {
+                case 0: tile_rt<0>(T, mode, sub, add, grid, h->s); break;
+                case 1: tile_rt<1>(T, mode, sub, add, grid, h->s); break;
+                default: tile_rt<2>(T, mode, sub, add, grid, h->s); break;
+            }
+        }
+        CU(h, cudaGetLastError());
+        h->st.launches++;
+        if (kind == K_CSC) h->st.sweep_csc_launches++;
+        else h->st.sweep_csr_launches++;
+        return CDMF_OK;
+    }
     const unsigned grid = D.nx + D.nc + D.nwb + D.ntb;
     if (grid == 0) return CDMF_OK;
     {
@@ -448,6 +542,68 @@ int reset_residual(cdmf_handle* h, void* dst, const float* src) {
     return CDMF_OK;
 }
 
+// One outer iteration (src/cdmf_ref.cpp:69-137): refresh (16-bit modes),
+// k rank-one updates, test RMSE into rmse_dst.
+int do_outer(cdmf_handle* h, int oiter, double* rmse_dst) {
+    int r;
+    if (h->rt != 0 && oiter > 1 && h->nnz > 0)
+        if ((r = refresh_residual(h))) return r;
+    for (uint32_t t = 0; t < h->o.k; ++t)
+        if ((r = feature_step(h, t, oiter))) return r;
+    if (h->o.rmse_each_outer && h->nt > 0)
+        if ((r = launch_rmse(h, rmse_dst))) return r;
+    return CDMF_OK;
+}
+
+// The same outer iteration replayed from a CUDA graph.  The launch sequence
+// depends only on (first outer, pending feature, P validity, refresh, RMSE),
+// so one graph per signature is captured on first use and replayed after.
+int do_outer_graph(cdmf_handle* h, int oiter, double* rmse_dst) {
+    const bool want_refresh = h->rt != 0 && oiter > 1 && h->nnz > 0;
+    const bool want_rmse = h->o.rmse_each_outer && h->nt > 0;
+    const int sig[5] = {oiter == 1, h->pending, h->p_for, want_refresh, want_rmse};
+    cdmf_handle::Graph* G = nullptr;
+    for (auto& g : h->graphs)
+        if (std::memcmp(g.sig, sig, sizeof(sig)) == 0) G = &g;
+    if (!G) {
+        const cdmf_stats before = h->st;
+        CU(h, cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+        const int r = do_outer(h, oiter, h->rmse_graph_slot);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->s, &graph);
+        if (r || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return r ? r : fail(h, CDMF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        }
+        cdmf_handle::Graph g;
+        std::memcpy(g.sig, sig, sizeof(sig));
+        const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) return fail(h, CDMF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+        g.end_pending = h->pending;
+        g.end_p_for = h->p_for;
+        g.launches = h->st.launches - before.launches;
+        g.csc = h->st.sweep_csc_launches - before.sweep_csc_launches;
+        g.csr = h->st.sweep_csr_launches - before.sweep_csr_launches;
+        g.rmse = h->st.rmse_launches - before.rmse_launches;
+        g.refresh = h->st.refresh_launches - before.refresh_launches;
+        h->graphs.push_back(g);
+        G = &h->graphs.back();
+    } else {
+        h->pending = G->end_pending;
+        h->p_for = G->end_p_for;
+        if (want_refresh) h->refreshed = true;
+        h->st.launches += G->launches;
+        h->st.sweep_csc_launches += G->csc;
+        h->st.sweep_csr_launches += G->csr;
+        h->st.rmse_launches += G->rmse;
+        h->st.refresh_launches += G->refresh;
+    }
+    CU(h, cudaGraphLaunch(G->exec, h->s));
+    if (want_rmse) CU(h, cudaMemcpyAsync(rmse_dst, h->rmse_graph_slot, sizeof(double), cudaMemcpyDeviceToDevice, h->s));
+    return CDMF_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -494,6 +650,7 @@ void cdmf_cuda_destroy(cdmf_handle* h) {
     cudaGetDevice(&dev);
     cudaSetDevice(h->o.device);
     if (h->s) cudaStreamSynchronize(h->s);
+    for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
     for (void* p : h->allocs) cudaFree(p);
     for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
     if (h->ev_start) cudaEventDestroy(h->ev_start);
@@ -551,6 +708,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         return bail(r);
     h->rmse_grid = (int)std::max<int64_t>(1, std::min<int64_t>(4 * 152, (h->nt + kBlock - 1) / kBlock));
     if ((r = dalloc(h, &h->rmse_part, h->rmse_grid)) || (r = dalloc(h, &h->rmse_out, 1 + std::max(0, o->maxiter))) ||
+        (r = dalloc(h, &h->rmse_graph_slot, 1)) ||
         (r = dalloc(h, &h->rmse_count, 1)))
         return bail(r);
     auto up = [&](void* dst, const void* src, size_t bytes) -> int {
@@ -597,6 +755,10 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     BinCfg cfg;
     if ((r = upload_bins(h, h->csr, plan_bins(p->csr_row_ptr, m, seq, cfg))) ||
         (r = upload_bins(h, h->csc, plan_bins(p->csc_col_ptr, n, seq, cfg))))
+        return bail(r);
+    h->tiles = o->version == 3 && !seq;
+    if (h->tiles && ((r = upload_tiles(h, h->tcsr, p->csr_row_ptr, m, N)) ||
+                     (r = upload_tiles(h, h->tcsc, p->csc_col_ptr, n, N))))
         return bail(r);
     // fresh state: W := 0 until set, H := 0, residual := ratings
     if (cudaMemsetAsync(h->W, 0, sizeof(float) * k * m, h->s) != cudaSuccess ||
@@ -653,19 +815,10 @@ int cdmf_cuda_run(cdmf_handle* h, int n_outer, double* rmse_out) {
         const int chunk = std::min(n_outer - done, slots);
         for (int q = 0; q < chunk; ++q) {
             const int oiter = h->next_oiter;
-            if (h->rt != 0 && oiter > 1 && h->nnz > 0) {
-                int r = refresh_residual(h);
-                if (r) return r;
-            }
-            for (uint32_t t = 0; t < h->o.k; ++t) {
-                int r = feature_step(h, t, oiter);
-                if (r) return r;
-            }
+            const int r = (h->o.use_graph && !h->profiling) ? do_outer_graph(h, oiter, h->rmse_out + q)
+                                                            : do_outer(h, oiter, h->rmse_out + q);
+            if (r) return r;
             h->st.updates += h->o.k;
-            if (h->o.rmse_each_outer && h->nt > 0) {
-                int r = launch_rmse(h, h->rmse_out + q);
-                if (r) return r;
-            }
             h->next_oiter++;
         }
         if (rmse_out && h->o.rmse_each_outer && h->nt > 0) {

@@ -14,7 +14,7 @@ Two reduction modes:
                   fro(gpu - ref32) <= 2 * fro(ref32 - ref64) + 1e-6
                   fro(gpu - ref64) <= 1.5 * fro(ref32 - ref64) + 1e-7
                   elementwise rel(gpu, ref32) <= 2 * rel(ref32, ref64) + 1e-5
-                  |rmse_gpu - rmse_ref32| <= 1e-5
+                  |rmse_gpu - rmse_ref32| <= max(1e-5, 2 * |rmse_ref32 - rmse_ref64|)
                 fro(x - r) = ||x - r||_F / ||r||_F; rel(x, r) = max |x - r| /
                 max(|r|, 0.1 * rms of r's feature vector).
 """
@@ -80,13 +80,18 @@ def test_sequential_bit_exact_each_outer(name):
     assert np.array_equal(bits(st["res_csr"]), bits(z["res_csr"]))
 
 
+def rmse_ok(got, r32, r64):
+    return abs(got - r32) <= max(RMSE_ATOL, 2 * abs(r32 - r64))
+
+
+@pytest.mark.parametrize("version", [1, 3])
 @pytest.mark.parametrize("name", ["simple", "tricky_simple", "mini"])
-def test_tree_within_fp32_budget_each_outer(name):
+def test_tree_within_fp32_budget_each_outer(name, version):
     R, z = load_golden(name)
     md = META[name]
     r64 = oracle.ccdpp(R, z["W0"].astype(np.float64), md["k"], md["lam"], md["maxiter"], md["maxinner"],
                        dtype=np.float64, history=True)
-    with engine.Engine(R, md["k"], md["lam"], md["maxiter"], md["maxinner"]) as e:
+    with engine.Engine(R, md["k"], md["lam"], md["maxiter"], md["maxinner"], version=version) as e:
         e.set_factors(z["W0"])
         for j in range(md["maxiter"]):
             rm = e.run(1)
@@ -94,7 +99,7 @@ def test_tree_within_fp32_budget_each_outer(name):
             okw, gw = within_budget(W, z["W_hist"][j], r64["W_hist"][j])
             okh, gh = within_budget(H, z["H_hist"][j], r64["H_hist"][j])
             assert okw and okh, (j, gw, gh)
-            assert abs(rm[0] - z["rmse"][j]) <= RMSE_ATOL
+            assert rmse_ok(rm[0], z["rmse"][j], r64["rmse"][j]), (rm[0], z["rmse"][j], r64["rmse"][j])
 
 
 def test_one_shot_train_matches_handle_api():
@@ -130,7 +135,8 @@ def test_cpu_scale_sequential_bit_exact(cpu_scale):
     assert np.array_equal(bits(st["res_csr"]), bits(ref["res_csr"]))
 
 
-def test_cpu_scale_tree_one_step_parity(cpu_scale):
+@pytest.mark.parametrize("version", [1, 3])
+def test_cpu_scale_tree_one_step_parity(cpu_scale, version):
     """From the oracle's state after outer j, one GPU outer iteration lands
     within the FP32 budget of the oracle's outer j+1 (errors do not compound)."""
     R, run, W0, ref = cpu_scale
@@ -138,7 +144,7 @@ def test_cpu_scale_tree_one_step_parity(cpu_scale):
     W = W0.copy()
     H = np.zeros((k, R.n), np.float32)
     rc, rr = R.csc_val.copy(), R.csr_val.copy()
-    with engine.Engine(R, k, lam, run["maxiter"], T) as e:
+    with engine.Engine(R, k, lam, run["maxiter"], T, version=version) as e:
         for j in range(1, run["maxiter"] + 1):
             e.set_state(W, H, rc, rr, j)
             rm = e.run(1)
@@ -150,16 +156,17 @@ def test_cpu_scale_tree_one_step_parity(cpu_scale):
             okw, gw = within_budget(Wg, W, W64)
             okh, gh = within_budget(Hg, H, H64)
             assert okw and okh, (j, gw, gh)
-            assert abs(rm[0] - oracle.rmse(R, W, H, k)) <= RMSE_ATOL
+            assert rmse_ok(rm[0], oracle.rmse(R, W, H, k), oracle.rmse(R, W64, H64, k))
 
 
-def test_cpu_scale_tree_free_running(cpu_scale):
+@pytest.mark.parametrize("version", [1, 3])
+def test_cpu_scale_tree_free_running(cpu_scale, version):
     R, run, W0, ref = cpu_scale
-    with engine.Engine(R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"]) as e:
+    with engine.Engine(R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"], version=version) as e:
         e.set_factors(W0)
         rm = e.run(run["maxiter"])
         W, H = e.factors()
-    assert np.max(np.abs(rm - ref["rmse"])) <= RMSE_ATOL, (rm, ref["rmse"])
+    assert all(rmse_ok(a, b, c) for a, b, c in zip(rm, ref["rmse"], ref["f64"]["rmse"])), (rm, ref["rmse"])
     okw, gw = within_budget(W, ref["W"], ref["f64"]["W"])
     okh, gh = within_budget(H, ref["H"], ref["f64"]["H"])
     assert okw and okh, (gw, gh)
@@ -193,14 +200,15 @@ def test_state_roundtrip_continues_identically():
     assert np.array_equal(bits(W), bits(z["W_hist"][3])) and np.array_equal(bits(H), bits(z["H_hist"][3]))
 
 
-def test_split_lines_within_fp32_budget():
+@pytest.mark.parametrize("version", [1, 3])
+def test_split_lines_within_fp32_budget(version):
     # a matrix with very long columns exercises the split-line bin (> 16384 nnz)
     R = synth.generate(m=60000, n=40, nnz_total=900000, test_fraction=0.01, row_alpha=0.5, row_min=1, row_max=40,
                        col_alpha=0.3, col_cap=60000, rank=4, seed=21)
     W0 = synth.initial_w(4, R.m, seed=1)
     ref = oracle.ccdpp(R, W0, 4, 0.05, 2, 2, threads=8, history=True)
     r64 = oracle.ccdpp(R, W0.astype(np.float64), 4, 0.05, 2, 2, threads=8, dtype=np.float64, history=True)
-    with engine.Engine(R, 4, 0.05, 2, 2) as e:
+    with engine.Engine(R, 4, 0.05, 2, 2, version=version) as e:
         c, _ = e.bins("csc")
         assert c[3] > 0, c
         e.set_factors(W0)
@@ -210,9 +218,107 @@ def test_split_lines_within_fp32_budget():
             okw, gw = within_budget(W, ref["W_hist"][j], r64["W_hist"][j])
             okh, gh = within_budget(H, ref["H_hist"][j], r64["H_hist"][j])
             assert okw and okh, (j, gw, gh)
-            assert abs(rm[0] - ref["rmse"][j]) <= RMSE_ATOL
+            assert rmse_ok(rm[0], ref["rmse"][j], r64["rmse"][j]), (rm[0], ref["rmse"][j], r64["rmse"][j])
     with engine.Engine(R, 4, 0.05, 2, 2, reduce="sequential") as e:
         e.set_factors(W0)
         e.run(2)
         W, H = e.factors()
     assert np.array_equal(bits(W), bits(ref["W"])) and np.array_equal(bits(H), bits(ref["H"]))
+
+
+@pytest.mark.parametrize("version", [1, 3])
+@pytest.mark.parametrize("residual", ["bf16", "f16"])
+def test_mixed_residual_rmse_vs_fp64_oracle(cpu_scale, residual, version):
+    """16-bit residual storage with FP32 factors and accumulation and a
+    per-outer-iteration FP32 refresh: test RMSE within 1e-3 of the FP64
+    oracle after every outer iteration."""
+    R, run, W0, ref = cpu_scale
+    r64 = oracle.ccdpp(R, W0.astype(np.float64), run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"],
+                       threads=8, dtype=np.float64)
+    with engine.Engine(R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"], residual=residual,
+                       version=version) as e:
+        e.set_factors(W0)
+        rm = e.run(run["maxiter"])
+        st = e.stats()
+        state = e.state()
+    assert np.max(np.abs(rm - r64["rmse"])) <= 1e-3, (rm, r64["rmse"])
+    assert st["refresh_launches"] == run["maxiter"] - 1 and st["nonfinite"] == 0
+    assert 0.0 < st["drift_rms"] < 5e-2, st["drift_rms"]
+    # both residual copies hold the same values (CSC order vs CSR order)
+    from cdmf_gb300 import _lib
+    import ctypes
+    perm = np.empty(R.nnz, np.uint32)
+    cp, ci = np.empty(R.n + 1, np.uint32), np.empty(R.nnz, np.uint32)
+    U = ctypes.c_uint32
+    _lib.load().cdmf_csr_to_csc(R.m, R.n, R.nnz, _lib.ptr(R.csr_ptr, U), _lib.ptr(R.csr_idx, U), None,
+                                _lib.ptr(cp, U), _lib.ptr(ci, U), None, _lib.ptr(perm, U))
+    assert np.array_equal(bits(state["res_csc"]), bits(state["res_csr"][perm]))
+
+
+def test_mixed_refresh_restores_exact_residual(cpu_scale):
+    """Right after a refresh the stored residual is R - W^T H rounded once to
+    BF16 (checked against a float64 recomputation on the host)."""
+    R, run, W0, ref = cpu_scale
+    with engine.Engine(R, run["k"], run["lambda_"], 3, 1, residual="bf16") as e:
+        e.set_factors(W0)
+        e.run(2)
+        e.set_profiling(False)
+        st = e.state()
+    W, H = st["W"].astype(np.float64), st["H"].astype(np.float64)
+    rows, cols, vals = R.coo()
+    exact = vals.astype(np.float64) - np.einsum("ti,ti->i", W[:, rows], H[:, cols])
+    got = st["res_csr"].astype(np.float64)
+    # after 2 outer iterations the residual went through one refresh and k
+    # further BF16 updates: it stays within a few BF16 ulps of the exact one
+    err = np.abs(got - exact)
+    assert np.sqrt(np.mean(err ** 2)) < 2e-2 and np.max(err) < 0.25
+
+
+@pytest.mark.parametrize("version", [1, 3])
+@pytest.mark.parametrize("residual", ["f32", "bf16"])
+def test_graph_replay_identical(cpu_scale, residual, version):
+    """Outer iterations replayed from CUDA graphs give bit-identical factors
+    and RMSE to the eagerly launched schedule."""
+    R, run, W0, ref = cpu_scale
+    out = []
+    for graph in (False, True):
+        with engine.Engine(R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"], residual=residual,
+                           use_graph=graph, version=version) as e:
+            e.set_factors(W0)
+            rm = e.run(run["maxiter"])
+            W, H = e.factors()
+            out.append((W, H, rm, e.stats()))
+    (W0_, H0_, r0, s0), (W1, H1, r1, s1) = out
+    assert np.array_equal(bits(W0_), bits(W1)) and np.array_equal(bits(H0_), bits(H1))
+    assert np.array_equal(r0, r1)
+    assert s0["launches"] == s1["launches"]
+
+
+@pytest.mark.parametrize("k,T", [(1, 3), (3, 1)])
+def test_tile_version_small_rank_within_budget(k, T):
+    R, z = load_golden("mini")
+    W0 = synth.initial_w(k, R.m, seed=5)
+    ref = oracle.ccdpp(R, W0, k, 0.1, 3, T, history=True)
+    r64 = oracle.ccdpp(R, W0.astype(np.float64), k, 0.1, 3, T, dtype=np.float64, history=True)
+    with engine.Engine(R, k, 0.1, 3, T, version=3) as e:
+        e.set_factors(W0)
+        for j in range(3):
+            rm = e.run(1)
+            W, H = e.factors()
+            okw, gw = within_budget(W, ref["W_hist"][j], r64["W_hist"][j])
+            okh, gh = within_budget(H, ref["H_hist"][j], r64["H_hist"][j])
+            assert okw and okh, (j, gw, gh)
+            assert rmse_ok(rm[0], ref["rmse"][j], r64["rmse"][j])
+
+
+def test_tile_version_deterministic():
+    R, z = load_golden("mini")
+    md = META["mini"]
+    outs = []
+    for _ in range(2):
+        with engine.Engine(R, md["k"], md["lam"], md["maxiter"], md["maxinner"], version=3) as e:
+            e.set_factors(z["W0"])
+            e.run(md["maxiter"])
+            outs.append(e.state())
+    for f in ("W", "H", "res_csc", "res_csr"):
+        assert np.array_equal(bits(outs[0][f]), bits(outs[1][f])), f
