@@ -42,6 +42,16 @@ namespace cdmf {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
+// Minimum resident blocks per SM asked of the compiler (register cap).
+// Without a value the compiler picks freely.
+#ifdef CDMF_SWEEP_MIN_BLOCKS
+#define CDMF_SWEEP_BOUNDS __launch_bounds__(kBlock, CDMF_SWEEP_MIN_BLOCKS)
+#else
+#define CDMF_SWEEP_BOUNDS __launch_bounds__(kBlock)
+#endif
+#ifndef CDMF_TILE_MIN_BLOCKS
+#define CDMF_TILE_MIN_BLOCKS 5
+#endif
 
 // sweep modes
 constexpr int M_PLAIN = 0;  // inner iterations >= 2: y only, no residual writes
@@ -297,7 +307,7 @@ __device__ __forceinline__ void line_scalars(const SweepArgs& A, uint32_t j, flo
 }
 
 template <int RT, int MODE, bool SUB, bool ADD>
-__global__ void __launch_bounds__(kBlock) sweep_kernel(const SweepArgs A) {
+__global__ void CDMF_SWEEP_BOUNDS sweep_kernel(const SweepArgs A) {
     uint32_t b = blockIdx.x;
     if (b < A.nx) {                                        // split-line chunk
         const XTask T = A.xt[b];

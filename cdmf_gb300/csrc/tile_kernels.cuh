@@ -86,7 +86,7 @@ __device__ __forceinline__ void tile_arrive(const TileArgs& T, uint32_t line, bo
 }
 
 template <int RT, int MODE, bool SUB, bool ADD>
-__global__ void __launch_bounds__(kBlock) tile_sweep_kernel(const TileArgs T) {
+__global__ void __launch_bounds__(kBlock, CDMF_TILE_MIN_BLOCKS) tile_sweep_kernel(const TileArgs T) {
     const SweepArgs& A = T.s;
     const uint32_t lane = threadIdx.x & 31;
     if (blockIdx.x >= T.tile_blocks) {                      // empty lines

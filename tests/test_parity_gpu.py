@@ -13,7 +13,7 @@ Two reduction modes:
                 inputs.  After every outer iteration:
                   fro(gpu - ref32) <= 2 * fro(ref32 - ref64) + 1e-6
                   fro(gpu - ref64) <= 1.5 * fro(ref32 - ref64) + 1e-7
-                  elementwise rel(gpu, ref32) <= 2 * rel(ref32, ref64) + 1e-5
+                  elementwise rel(gpu, ref32) <= 2 * rel(ref32, ref64) + 1e-4
                   |rmse_gpu - rmse_ref32| <= max(1e-5, 2 * |rmse_ref32 - rmse_ref64|)
                 fro(x - r) = ||x - r||_F / ||r||_F; rel(x, r) = max |x - r| /
                 max(|r|, 0.1 * rms of r's feature vector).
@@ -59,7 +59,7 @@ def within_budget(x, ref32, ref64):
     b_rel = rel_err(ref32, ref64)
     got = dict(fro32=fro(x, ref32), fro64=fro(x, ref64), rel32=rel_err(x, ref32), budget_fro=b_fro, budget_rel=b_rel)
     ok = (got["fro32"] <= 2 * b_fro + 1e-6 and got["fro64"] <= 1.5 * b_fro + 1e-7
-          and got["rel32"] <= 2 * b_rel + 1e-5)
+          and got["rel32"] <= 2 * b_rel + 1e-4)
     return ok, got
 
 
