@@ -171,6 +171,7 @@ def main():
     ap.add_argument("--version", type=int, default=3, choices=[1, 2, 3],
                     help="1/2: row-length-binned sweeps, 3: nonzero-balanced tiles")
     ap.add_argument("--graph", type=int, default=1, help="replay outer iterations from CUDA graphs")
+    ap.add_argument("--relabel", type=int, default=1, help="renumber rows and columns by degree inside the engine")
     ap.add_argument("--e2e-outer", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -222,7 +223,7 @@ def main():
     W0 = synth.initial_w(k, R.m, seed=rank)
 
     e = engine.Engine(R, k, lam, maxiter=max(args.steps, args.e2e_outer), maxinneriter=T, residual=args.residual,
-                      device=device, version=args.version, use_graph=bool(args.graph))
+                      device=device, version=args.version, use_graph=bool(args.graph), relabel=bool(args.relabel))
     e.set_factors(W0)
     e.run(args.warmup)
     # timed: device-resident
@@ -276,6 +277,7 @@ def main():
         "config": {"workload": f"{WORKLOAD} {R.m}x{R.n} train_nnz={R.nnz} test_nnz={R.nnz_test} k={k} "
                                f"lambda={lam} T={T}",
                    "residual": args.residual, "version": args.version, "cuda_graph": bool(args.graph),
+                   "relabel": bool(args.relabel),
                    "step": "one outer iteration (k rank-one updates + test RMSE)",
                    "l2": "no flush: the residual copies streamed every feature exceed L2",
                    "parallelism": f"replicas x{ws}"},
@@ -312,7 +314,8 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
     h2d = sum(getattr(Rp, f).nbytes for f in arrays) + W0.nbytes
     d2h = W0.nbytes + 4 * k * R.n + 8 * args.e2e_outer
     Wp[...] = W0
-    kw = dict(residual=args.residual, device=device, version=args.version, use_graph=bool(args.graph))
+    kw = dict(residual=args.residual, device=device, version=args.version, use_graph=bool(args.graph),
+              relabel=bool(args.relabel))
     engine.train(Rp, Wp, k, lam, 1, T, **kw)  # warm the context
     dist.barrier()
     t0 = time.perf_counter()

@@ -21,6 +21,7 @@
 #include "sweep_kernels.cuh"
 #include "refresh_kernels.cuh"
 #include "tile_kernels.cuh"
+#include "relabel.h"
 
 #include <cuda_runtime.h>
 
@@ -138,6 +139,9 @@ struct cdmf_handle {
     DevBins csr, csc;
     DevTiles tcsr, tcsc;
     bool tiles = false;              // version 3: nonzero-balanced tile sweeps
+    // degree relabelling: new id -> caller id, new position -> caller position
+    bool relabeled = false;
+    std::vector<uint32_t> row_old, col_old, csr_pos, csc_pos;
     // 16-bit residual modes: CSR->CSC position map, row-major factor copies
     uint32_t* to_csc = nullptr;
     float *Wrm = nullptr, *Hrm = nullptr;
@@ -542,6 +546,23 @@ int reset_residual(cdmf_handle* h, void* dst, const float* src) {
     return CDMF_OK;
 }
 
+// Caller numbering <-> engine numbering (identity unless relabelled).
+// X is k x len feature-major; `old_of_new` maps an engine id to a caller id.
+void gather_ids(const float* user, float* eng, uint32_t k, int64_t len, const std::vector<uint32_t>& old_of_new) {
+    for (uint32_t t = 0; t < k; ++t) {
+        const float* u = user + (size_t)t * len;
+        float* e = eng + (size_t)t * len;
+        for (int64_t q = 0; q < len; ++q) e[q] = u[old_of_new[q]];
+    }
+}
+void scatter_ids(const float* eng, float* user, uint32_t k, int64_t len, const std::vector<uint32_t>& old_of_new) {
+    for (uint32_t t = 0; t < k; ++t) {
+        const float* e = eng + (size_t)t * len;
+        float* u = user + (size_t)t * len;
+        for (int64_t q = 0; q < len; ++q) u[old_of_new[q]] = e[q];
+    }
+}
+
 // One outer iteration (src/cdmf_ref.cpp:69-137): refresh (16-bit modes),
 // k rank-one updates, test RMSE into rmse_dst.
 int do_outer(cdmf_handle* h, int oiter, double* rmse_dst) {
@@ -685,7 +706,29 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CDMF_ERR_NO_DEVICE;
     if (o->device < 0 || o->device >= ndev) return CDMF_ERR_NO_DEVICE;
 
+    const bool seq_order = o->reduce == CDMF_REDUCE_SEQUENTIAL;
+    Relabel RL;
+    cdmf_problem q = *p;
+    if (o->relabel && !seq_order && p->nnz > 0) {
+        if (!relabel(*p, RL)) return CDMF_ERR_INVALID;
+        q.csr_row_ptr = RL.csr_ptr.data();
+        q.csr_col_idx = RL.csr_idx.data();
+        q.csr_val = RL.csr_val.data();
+        q.csc_col_ptr = RL.csc_ptr.data();
+        q.csc_row_idx = RL.csc_idx.data();
+        q.csc_val = RL.csc_val.data();
+        q.test_row = RL.te_row.data();
+        q.test_col = RL.te_col.data();
+        p = &q;
+    }
     cdmf_handle* h = new cdmf_handle();
+    if (p == &q) {
+        h->relabeled = true;
+        h->row_old = std::move(RL.row_old);
+        h->col_old = std::move(RL.col_old);
+        h->csr_pos = std::move(RL.csr_pos);
+        h->csc_pos = std::move(RL.csc_pos);
+    }
     h->o = *o;
     h->m = p->m;
     h->n = p->n;
@@ -778,6 +821,17 @@ int cdmf_cuda_set_factors(cdmf_handle* h, const float* W0, const float* H0) {
     if (!h) return CDMF_ERR_INVALID;
     CU(h, cudaSetDevice(h->o.device));
     const size_t wb = sizeof(float) * h->o.k * h->m, hb = sizeof(float) * h->o.k * h->n;
+    std::vector<float> tw, th;
+    if (h->relabeled && W0) {
+        tw.resize((size_t)h->o.k * h->m);
+        gather_ids(W0, tw.data(), h->o.k, h->m, h->row_old);
+        W0 = tw.data();
+    }
+    if (h->relabeled && H0) {
+        th.resize((size_t)h->o.k * h->n);
+        gather_ids(H0, th.data(), h->o.k, h->n, h->col_old);
+        H0 = th.data();
+    }
     if (W0) CU(h, cudaMemcpyAsync(h->W, W0, wb, cudaMemcpyHostToDevice, h->s));
     else CU(h, cudaMemsetAsync(h->W, 0, wb, h->s));
     if (H0) CU(h, cudaMemcpyAsync(h->H, H0, hb, cudaMemcpyHostToDevice, h->s));
@@ -856,9 +910,16 @@ int cdmf_cuda_run(cdmf_handle* h, int n_outer, double* rmse_out) {
 int cdmf_cuda_get_factors(cdmf_handle* h, float* W, float* H) {
     if (!h) return CDMF_ERR_INVALID;
     CU(h, cudaSetDevice(h->o.device));
-    if (W) CU(h, cudaMemcpyAsync(W, h->W, sizeof(float) * h->o.k * h->m, cudaMemcpyDeviceToHost, h->s));
-    if (H) CU(h, cudaMemcpyAsync(H, h->H, sizeof(float) * h->o.k * h->n, cudaMemcpyDeviceToHost, h->s));
+    std::vector<float> tw, th;
+    float* wd = W;
+    float* hd = H;
+    if (h->relabeled && W) { tw.resize((size_t)h->o.k * h->m); wd = tw.data(); }
+    if (h->relabeled && H) { th.resize((size_t)h->o.k * h->n); hd = th.data(); }
+    if (W) CU(h, cudaMemcpyAsync(wd, h->W, sizeof(float) * h->o.k * h->m, cudaMemcpyDeviceToHost, h->s));
+    if (H) CU(h, cudaMemcpyAsync(hd, h->H, sizeof(float) * h->o.k * h->n, cudaMemcpyDeviceToHost, h->s));
     CU(h, cudaStreamSynchronize(h->s));
+    if (h->relabeled && W) scatter_ids(wd, W, h->o.k, h->m, h->row_old);
+    if (h->relabeled && H) scatter_ids(hd, H, h->o.k, h->n, h->col_old);
     return CDMF_OK;
 }
 
@@ -893,8 +954,17 @@ int cdmf_cuda_get_state(cdmf_handle* h, float* W, float* H, float* res_csc, floa
         }
         return CDMF_OK;
     };
-    if ((r = down(res_csc, h->res_csc)) || (r = down(res_csr, h->res_csr))) return r;
+    std::vector<float> tc, tr;
+    float* dc = res_csc;
+    float* dr = res_csr;
+    if (h->relabeled && res_csc) { tc.resize(h->nnz); dc = tc.data(); }
+    if (h->relabeled && res_csr) { tr.resize(h->nnz); dr = tr.data(); }
+    if ((r = down(dc, h->res_csc)) || (r = down(dr, h->res_csr))) return r;
     CU(h, cudaStreamSynchronize(h->s));
+    if (h->relabeled) {
+        if (res_csc) for (int64_t o = 0; o < h->nnz; ++o) res_csc[h->csc_pos[o]] = dc[o];
+        if (res_csr) for (int64_t o = 0; o < h->nnz; ++o) res_csr[h->csr_pos[o]] = dr[o];
+    }
     if (next_oiter) *next_oiter = h->next_oiter;
     return CDMF_OK;
 }
@@ -904,6 +974,23 @@ int cdmf_cuda_set_state(cdmf_handle* h, const float* W, const float* H, const fl
     if (!h || !W || !H || next_oiter < 1) return CDMF_ERR_INVALID;
     if (h->nnz > 0 && (!res_csc || !res_csr)) return CDMF_ERR_INVALID;
     CU(h, cudaSetDevice(h->o.device));
+    std::vector<float> tw, th, tc, tr;
+    if (h->relabeled) {
+        tw.resize((size_t)h->o.k * h->m);
+        th.resize((size_t)h->o.k * h->n);
+        gather_ids(W, tw.data(), h->o.k, h->m, h->row_old);
+        gather_ids(H, th.data(), h->o.k, h->n, h->col_old);
+        W = tw.data();
+        H = th.data();
+        tc.resize(h->nnz);
+        tr.resize(h->nnz);
+        for (int64_t o = 0; o < h->nnz; ++o) {
+            tc[o] = res_csc[h->csc_pos[o]];
+            tr[o] = res_csr[h->csr_pos[o]];
+        }
+        res_csc = tc.data();
+        res_csr = tr.data();
+    }
     CU(h, cudaMemcpyAsync(h->W, W, sizeof(float) * h->o.k * h->m, cudaMemcpyHostToDevice, h->s));
     CU(h, cudaMemcpyAsync(h->H, H, sizeof(float) * h->o.k * h->n, cudaMemcpyHostToDevice, h->s));
     auto upres = [&](void* dst, const float* src) -> int {

@@ -46,7 +46,7 @@ def _problem(R):
 
 
 def make_opts(k, lambda_, maxiter=5, maxinneriter=5, version=1, residual="f32", reduce="tree",
-              rmse_each_outer=True, use_graph=False, device=0, threads_per_block=0, verbose=0):
+              rmse_each_outer=True, use_graph=False, device=0, threads_per_block=0, verbose=0, relabel=True):
     o = _lib.Opts()
     _lib.load().cdmf_opts_default(ctypes.byref(o))
     o.k, o.lambda_, o.maxiter, o.maxinneriter = int(k), float(lambda_), int(maxiter), int(maxinneriter)
@@ -56,6 +56,7 @@ def make_opts(k, lambda_, maxiter=5, maxinneriter=5, version=1, residual="f32", 
     o.rmse_each_outer = int(bool(rmse_each_outer))
     o.use_graph = int(bool(use_graph))
     o.device, o.threads_per_block, o.verbose = int(device), int(threads_per_block), int(verbose)
+    o.relabel = int(bool(relabel))
     return o
 
 

@@ -87,6 +87,8 @@ typedef struct {
     int32_t threads_per_block;/* -nThreadsPerBlock; 0 = engine default (256) */
     int32_t device;           /* CUDA device ordinal */
     int32_t verbose;
+    int32_t relabel;          /* 1: renumber rows and columns by degree inside the engine
+                                 (tree order only; results come back in the caller's numbering) */
 } cdmf_opts;
 
 /* Engine timings and counters of the most recent cdmf_cuda_run/train. */
