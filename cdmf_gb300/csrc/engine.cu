@@ -36,11 +36,12 @@ using namespace cdmf;
 
 namespace {
 
+// bins: 0 thread, 1 8-lane group, 2 warp, 3 CTA, 4 split
 struct Bins {
     std::vector<XTask> x;
-    std::vector<uint32_t> c, w, t;
+    std::vector<uint32_t> c, w, g, t;
     uint32_t nslots = 0, nxl = 0;
-    int64_t count[4] = {0, 0, 0, 0}, nnz[4] = {0, 0, 0, 0};
+    int64_t count[5] = {0, 0, 0, 0, 0}, nnz[5] = {0, 0, 0, 0, 0};
 };
 
 // nonzero-balanced tiles of one compressed copy (version 3)
@@ -54,16 +55,17 @@ struct DevTiles {
 
 struct DevBins {
     XTask* x = nullptr;
-    uint32_t *c = nullptr, *w = nullptr, *t = nullptr;
+    uint32_t *c = nullptr, *w = nullptr, *g = nullptr, *t = nullptr;
     float2* part = nullptr;
     uint32_t* xcount = nullptr;
-    uint32_t nx = 0, nc = 0, nw = 0, nt = 0, nwb = 0, ntb = 0;
+    uint32_t nx = 0, nc = 0, nw = 0, ng = 0, nt = 0, nwb = 0, ngb = 0, ntb = 0;
     Bins host;
 };
 
 // Bin thresholds (line length in nonzeros).
 struct BinCfg {
     uint32_t thread_max = 12;    // <= : one thread per line
+    uint32_t group_max = 256;    // <= : one 8-lane group per line
     uint32_t warp_max = 2048;    // <= : one warp per line
     uint32_t cta_max = 16384;    // <= : one CTA per line; above: split
     uint32_t chunk = 8192;       // nonzeros per chunk of a split line
@@ -75,15 +77,17 @@ Bins plan_bins(const uint32_t* ptr, int64_t lines, bool sequential, const BinCfg
         const uint32_t len = ptr[j + 1] - ptr[j];
         int bin;
         if (sequential || len <= cfg.thread_max) bin = 0;
-        else if (len <= cfg.warp_max) bin = 1;
-        else if (len <= cfg.cta_max) bin = 2;
-        else bin = 3;
+        else if (len <= cfg.group_max) bin = 1;
+        else if (len <= cfg.warp_max) bin = 2;
+        else if (len <= cfg.cta_max) bin = 3;
+        else bin = 4;
         B.count[bin]++;
         B.nnz[bin] += len;
         switch (bin) {
             case 0: B.t.push_back((uint32_t)j); break;
-            case 1: B.w.push_back((uint32_t)j); break;
-            case 2: B.c.push_back((uint32_t)j); break;
+            case 1: B.g.push_back((uint32_t)j); break;
+            case 2: B.w.push_back((uint32_t)j); break;
+            case 3: B.c.push_back((uint32_t)j); break;
             default: {
                 const uint32_t nch = (len + cfg.chunk - 1) / cfg.chunk;
                 const uint32_t first = B.nslots;
@@ -216,16 +220,20 @@ int upload_bins(cdmf_handle* h, DevBins& D, Bins&& B) {
     D.nx = (uint32_t)B.x.size();
     D.nc = (uint32_t)B.c.size();
     D.nw = (uint32_t)B.w.size();
+    D.ng = (uint32_t)B.g.size();
     D.nt = (uint32_t)B.t.size();
     D.nwb = (D.nw + kWarps - 1) / kWarps;
+    D.ngb = (D.ng + kBlock / 8 - 1) / (kBlock / 8);
     D.ntb = (D.nt + kBlock - 1) / kBlock;
     int r;
     if ((r = dalloc(h, &D.x, B.x.size())) || (r = dalloc(h, &D.c, B.c.size())) || (r = dalloc(h, &D.w, B.w.size())) ||
-        (r = dalloc(h, &D.t, B.t.size())) || (r = dalloc(h, &D.part, B.nslots)) || (r = dalloc(h, &D.xcount, B.nxl)))
+        (r = dalloc(h, &D.g, B.g.size())) || (r = dalloc(h, &D.t, B.t.size())) || (r = dalloc(h, &D.part, B.nslots)) ||
+        (r = dalloc(h, &D.xcount, B.nxl)))
         return r;
     if (D.nx) CU(h, cudaMemcpyAsync(D.x, B.x.data(), sizeof(XTask) * D.nx, cudaMemcpyHostToDevice, h->s));
     if (D.nc) CU(h, cudaMemcpyAsync(D.c, B.c.data(), 4 * D.nc, cudaMemcpyHostToDevice, h->s));
     if (D.nw) CU(h, cudaMemcpyAsync(D.w, B.w.data(), 4 * D.nw, cudaMemcpyHostToDevice, h->s));
+    if (D.ng) CU(h, cudaMemcpyAsync(D.g, B.g.data(), 4 * D.ng, cudaMemcpyHostToDevice, h->s));
     if (D.nt) CU(h, cudaMemcpyAsync(D.t, B.t.data(), 4 * D.nt, cudaMemcpyHostToDevice, h->s));
     CU(h, cudaMemsetAsync(D.xcount, 0, 4 * std::max<uint32_t>(1, B.nxl), h->s));
     CU(h, cudaStreamSynchronize(h->s));  // host vectors are released below
@@ -233,6 +241,7 @@ int upload_bins(cdmf_handle* h, DevBins& D, Bins&& B) {
     D.host.x.clear(); D.host.x.shrink_to_fit();
     D.host.c.clear(); D.host.c.shrink_to_fit();
     D.host.w.clear(); D.host.w.shrink_to_fit();
+    D.host.g.clear(); D.host.g.shrink_to_fit();
     D.host.t.clear(); D.host.t.shrink_to_fit();
     return CDMF_OK;
 }
@@ -339,12 +348,15 @@ SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const
     A.xt = D.x;
     A.cl = D.c;
     A.wl = D.w;
+    A.gl = D.g;
     A.tl = D.t;
     A.nx = D.nx;
     A.nc = D.nc;
     A.nw = D.nw;
+    A.ng = D.ng;
     A.nt = D.nt;
     A.nwb = D.nwb;
+    A.ngb = D.ngb;
     A.part = D.part;
     A.xcount = D.xcount;
     return A;
@@ -380,7 +392,7 @@ int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A,
         else h->st.sweep_csr_launches++;
         return CDMF_OK;
     }
-    const unsigned grid = D.nx + D.nc + D.nwb + D.ntb;
+    const unsigned grid = D.nx + D.nc + D.nwb + D.ngb + D.ntb;
     if (grid == 0) return CDMF_OK;
     {
         Timed tm(h, kind);
@@ -1028,10 +1040,10 @@ int cdmf_cuda_stats(const cdmf_handle* h, cdmf_stats* s) {
     return CDMF_OK;
 }
 
-int cdmf_cuda_bins(const cdmf_handle* h, int which, int64_t counts[4], int64_t nnz[4]) {
+int cdmf_cuda_bins(const cdmf_handle* h, int which, int64_t counts[5], int64_t nnz[5]) {
     if (!h || (which != 0 && which != 1)) return CDMF_ERR_INVALID;
     const Bins& B = which == 0 ? h->csr.host : h->csc.host;
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 5; ++q) {
         if (counts) counts[q] = B.count[q];
         if (nnz) nnz[q] = B.nnz[q];
     }

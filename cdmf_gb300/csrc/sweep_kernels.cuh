@@ -32,6 +32,7 @@
 //                             in chunk order (deterministic, no float atomics)
 //   blocks [nx, nx+nc)        one line per CTA
 //   blocks [.., +nwb)         one line per warp
+//   blocks [.., +ngb)         one line per 8-lane group (4 lines per warp)
 //   blocks [.., +ntb)         one line per thread, index order = reference order
 #pragma once
 #include <cuda_bf16.h>
@@ -81,9 +82,11 @@ struct SweepArgs {
     const XTask* xt;
     const uint32_t* cl;
     const uint32_t* wl;
+    const uint32_t* gl;
     const uint32_t* tl;
-    uint32_t nx, nc, nw, nt;
+    uint32_t nx, nc, nw, ng, nt;
     uint32_t nwb;                  // blocks of the warp bin
+    uint32_t ngb;                  // blocks of the group bin (32 lines per block)
     float2* part;                  // split-line partials
     uint32_t* xcount;              // split-line arrival counters (left at 0)
 };
@@ -258,9 +261,10 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
     hs = h.value();
 }
 
+template <int WIDTH = 32>
 __device__ __forceinline__ void warp_sum2(float& g, float& h) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = WIDTH / 2; o > 0; o >>= 1) {
         g = __fadd_rn(g, __shfl_xor_sync(0xffffffffu, g, o));
         h = __fadd_rn(h, __shfl_xor_sync(0xffffffffu, h, o));
     }
@@ -366,6 +370,21 @@ __global__ void CDMF_SWEEP_BOUNDS sweep_kernel(const SweepArgs A) {
         return;
     }
     b -= A.nwb;
+    if (b < A.ngb) {                                       // one line per 8-lane group
+        const uint32_t slot = b * (kBlock / 8) + (threadIdx.x >> 3);
+        const uint32_t sub = threadIdx.x & 7;
+        const bool valid = slot < A.ng;
+        const uint32_t j = valid ? A.gl[slot] : 0u;
+        const uint32_t beg = valid ? A.ptr[j] : 0u, end = valid ? A.ptr[j + 1] : 0u;
+        float bj = 0.0f, dj = 0.0f;
+        if (valid) line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
+        float g = 0.0f, h = 0.0f;
+        strided<RT, MODE, SUB, ADD, 8, false>(A, beg, end, sub, bj, dj, g, h);
+        warp_sum2<8>(g, h);
+        if (valid && sub == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
+        return;
+    }
+    b -= A.ngb;
     const uint32_t t = b * kBlock + threadIdx.x;           // one line per thread
     if (t >= A.nt) return;
     const uint32_t j = A.tl[t];

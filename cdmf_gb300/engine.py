@@ -143,9 +143,9 @@ class Engine:
         return {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
 
     def bins(self, which):
-        """which: 'csr' or 'csc' -> (lines per bin, nnz per bin) for (thread, warp, cta, split)."""
-        c = (ctypes.c_int64 * 4)()
-        z = (ctypes.c_int64 * 4)()
+        """which: 'csr' or 'csc' -> (lines per bin, nnz per bin) for (thread, group8, warp, cta, split)."""
+        c = (ctypes.c_int64 * 5)()
+        z = (ctypes.c_int64 * 5)()
         check(self.lib.cdmf_cuda_bins(self.h, 0 if which == "csr" else 1, c, z), "cdmf_cuda_bins", self.h)
         return list(c), list(z)
 

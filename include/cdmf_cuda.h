@@ -156,9 +156,10 @@ int cdmf_cuda_stats(const cdmf_handle* h, cdmf_stats* s);
  * failure. */
 void* cdmf_cuda_host_alloc(uint64_t bytes);
 void cdmf_cuda_host_free(void* p);
-/* Row-length bins of the two sweeps: counts[4] of lines per bin
- * (thread, warp, CTA, split) and nnz[4] for CSR (which=0) or CSC (which=1). */
-int cdmf_cuda_bins(const cdmf_handle* h, int which, int64_t counts[4], int64_t nnz[4]);
+/* Row-length bins of the two sweeps: counts[5] of lines per bin
+ * (thread, 8-lane group, warp, CTA, split) and nnz[5] for CSR (which=0) or
+ * CSC (which=1). */
+int cdmf_cuda_bins(const cdmf_handle* h, int which, int64_t counts[5], int64_t nnz[5]);
 
 #ifdef __cplusplus
 }

@@ -210,7 +210,7 @@ def test_split_lines_within_fp32_budget(version):
     r64 = oracle.ccdpp(R, W0.astype(np.float64), 4, 0.05, 2, 2, threads=8, dtype=np.float64, history=True)
     with engine.Engine(R, 4, 0.05, 2, 2, version=version) as e:
         c, _ = e.bins("csc")
-        assert c[3] > 0, c
+        assert c[4] > 0, c
         e.set_factors(W0)
         for j in range(2):
             rm = e.run(1)
