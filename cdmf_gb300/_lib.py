@@ -93,6 +93,15 @@ EXPORTS = {
     "cdmf_cuda_host_alloc": (ctypes.c_void_p, [ctypes.c_uint64]),
     "cdmf_cuda_host_free": (None, [ctypes.c_void_p]),
     "cdmf_cuda_bins": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_i64p, c_i64p]),
+    "cdmf_cuda_batch_create": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Opts), ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_void_p)]),
+    "cdmf_cuda_batch_destroy": (None, [ctypes.c_void_p]),
+    "cdmf_cuda_batch_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "cdmf_cuda_batch_set_factors": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_f32p)]),
+    "cdmf_cuda_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_f64p]),
+    "cdmf_cuda_batch_run_sequential": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_f64p, c_f64p]),
+    "cdmf_cuda_batch_get_factors": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_f32p), ctypes.POINTER(c_f32p)]),
+    "cdmf_cuda_batch_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
     "cdmf_synth_create": (ctypes.c_int, [ctypes.POINTER(SynthSpec), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "cdmf_synth_info": (ctypes.c_int, [ctypes.c_void_p, c_i64p, c_i64p, c_i64p, c_i64p]),
     "cdmf_synth_copy": (ctypes.c_int, [ctypes.c_void_p, c_u32p, c_u32p, c_f32p, c_u32p, c_u32p, c_f32p,

@@ -409,60 +409,79 @@ int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A,
     return CDMF_OK;
 }
 
-// One feature t of outer iteration `oiter`.
-int feature_step(cdmf_handle* h, uint32_t t, int oiter) {
+// The two sweeps of inner iteration `it` of feature t: A over CSC (solves
+// H[t]), B over CSR (solves W[t]).
+void feature_args(cdmf_handle* h, uint32_t t, int it, SweepArgs& A, SweepArgs& B) {
     const int64_t m = h->m, n = h->n;
     const uint32_t k = h->o.k;
     float* Wt = h->W + (size_t)t * m;
     float* Ht = h->H + (size_t)t * n;
     const int tp = h->pending;
-    const bool sub = tp >= 0, add = oiter > 1;
-    const float* Wp = sub ? h->W + (size_t)tp * m : nullptr;
-    const float* Hp = sub ? h->H + (size_t)tp * n : nullptr;
-    const float* Wnext = h->W + (size_t)((t + 1) % k) * m;
+    const float* Wp = tp >= 0 ? h->W + (size_t)tp * m : nullptr;
+    const float* Hp = tp >= 0 ? h->H + (size_t)tp * n : nullptr;
+    const bool first = it == 1, last = it == h->o.maxinneriter;
+    // h_t over CSC: cross vectors are rows (length m)
+    A = base_args(h, h->csc, h->csc_ptr, h->csc_idx, h->res_csc);
+    A.out = Ht;
+    if (first) {
+        A.P = h->P;
+        A.b = Hp;
+        A.d = Ht;
+        A.emitQ = h->Q;
+    } else {
+        A.y = Wt;
+    }
+    // w_t over CSR: cross vectors are columns (length n)
+    B = base_args(h, h->csr, h->csr_ptr, h->csr_idx, h->res_csr);
+    B.out = Wt;
+    if (first) {
+        B.Q = h->Q;
+        B.b = Wp;
+        B.d = Wt;
+    } else {
+        B.y = Ht;
+    }
+    if (last) {
+        B.emitP = h->P;
+        B.next_old = h->W + (size_t)((t + 1) % k) * m;
+    }
+}
+
+// Makes P valid for feature t (it is, in steady state: the previous feature's
+// last CSR sweep wrote it).
+int feature_prepare(cdmf_handle* h, uint32_t t) {
+    if (h->p_for == (int)t) return CDMF_OK;
+    const int64_t m = h->m;
+    const int tp = h->pending;
+    if (m) {
+        pack_p_kernel<<<(unsigned)std::min<int64_t>(4096, (m + 255) / 256), 256, 0, h->s>>>(
+            h->P, tp >= 0 ? h->W + (size_t)tp * m : nullptr, h->W + (size_t)t * m, m);
+        CU(h, cudaGetLastError());
+        h->st.launches++;
+    }
+    h->p_for = (int)t;
+    return CDMF_OK;
+}
+
+void feature_finish(cdmf_handle* h, uint32_t t) {
+    h->p_for = (int)((t + 1) % h->o.k);
+    h->pending = (int)t;
+}
+
+// One feature t of outer iteration `oiter`.
+int feature_step(cdmf_handle* h, uint32_t t, int oiter) {
     const int T = h->o.maxinneriter;
     if (T <= 0) return CDMF_OK;
-    if (h->p_for != (int)t) {
-        if (m) {
-            pack_p_kernel<<<(unsigned)std::min<int64_t>(4096, (m + 255) / 256), 256, 0, h->s>>>(h->P, Wp, Wt, m);
-            CU(h, cudaGetLastError());
-            h->st.launches++;
-        }
-        h->p_for = (int)t;
-    }
+    const bool sub = h->pending >= 0, add = oiter > 1;
     int r;
+    if ((r = feature_prepare(h, t))) return r;
     for (int it = 1; it <= T; ++it) {
-        const bool first = it == 1, last = it == T;
-        // h_t over CSC: cross vectors are rows (length m)
-        SweepArgs A = base_args(h, h->csc, h->csc_ptr, h->csc_idx, h->res_csc);
-        A.out = Ht;
-        if (first) {
-            A.P = h->P;
-            A.b = Hp;
-            A.d = Ht;
-            A.emitQ = h->Q;
-        } else {
-            A.y = Wt;
-        }
-        if ((r = launch_sweep(h, K_CSC, h->csc, A, first ? M_CSC : M_PLAIN, sub, add))) return r;
-        // w_t over CSR: cross vectors are columns (length n)
-        SweepArgs B = base_args(h, h->csr, h->csr_ptr, h->csr_idx, h->res_csr);
-        B.out = Wt;
-        if (first) {
-            B.Q = h->Q;
-            B.b = Wp;
-            B.d = Wt;
-        } else {
-            B.y = Ht;
-        }
-        if (last) {
-            B.emitP = h->P;
-            B.next_old = Wnext;
-        }
-        if ((r = launch_sweep(h, K_CSR, h->csr, B, first ? M_CSR : M_PLAIN, sub, add))) return r;
+        SweepArgs A, B;
+        feature_args(h, t, it, A, B);
+        if ((r = launch_sweep(h, K_CSC, h->csc, A, it == 1 ? M_CSC : M_PLAIN, sub, add))) return r;
+        if ((r = launch_sweep(h, K_CSR, h->csr, B, it == 1 ? M_CSR : M_PLAIN, sub, add))) return r;
     }
-    h->p_for = (int)((t + 1) % k);
-    h->pending = (int)t;
+    feature_finish(h, t);
     return CDMF_OK;
 }
 
@@ -1118,6 +1137,446 @@ int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* 
     r = cdmf_cuda_get_factors(h, W, H);
     cdmf_cuda_destroy(h);
     return r;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Batches of independent factorisations (uneven sizes, own k and lambda).
+//
+// All problems advance in lockstep.  At feature index t, every problem with
+// k > t runs its sweep, and the sweeps of all those problems run in ONE
+// persistent launch (grouped_sweep_kernel): resident blocks pull
+// (problem, bin-block) work from a device queue.  The residual refresh,
+// the packed-table setup and the test RMSE stay per problem.  The whole
+// schedule of a run is planned on the host, its sweep descriptors are
+// uploaded once, and in graph mode the run is replayed as one CUDA graph.
+// ============================================================================
+
+namespace {
+
+enum { OP_PACK, OP_REFRESH, OP_GSWEEP, OP_FINISH, OP_RMSE };
+
+struct BatchOp {
+    int kind;
+    int q;            // problem (PACK, REFRESH, FINISH, RMSE)
+    uint32_t t;       // feature (PACK, FINISH)
+    int mode;         // GSWEEP
+    bool sub, add;
+    int side;         // K_CSC / K_CSR
+    uint32_t desc_off, nq, prefix_off, queue;
+    int slot;         // RMSE slot
+};
+
+template <int RT>
+void grouped_rt(int mode, bool sub, bool add, const SweepArgs* d, const uint32_t* pre, uint32_t nq, uint32_t* queue,
+                int grid, cudaStream_t s) {
+#define CDMF_G(M, S, A) grouped_sweep_kernel<RT, M, S, A><<<grid, kBlock, 0, s>>>(d, pre, nq, queue)
+    if (mode == M_PLAIN) CDMF_G(M_PLAIN, false, false);
+    else if (mode == M_CSC) {
+        if (sub && add) CDMF_G(M_CSC, true, true);
+        else if (sub) CDMF_G(M_CSC, true, false);
+        else if (add) CDMF_G(M_CSC, false, true);
+        else CDMF_G(M_CSC, false, false);
+    } else {
+        if (sub && add) CDMF_G(M_CSR, true, true);
+        else if (sub) CDMF_G(M_CSR, true, false);
+        else if (add) CDMF_G(M_CSR, false, true);
+        else CDMF_G(M_CSR, false, false);
+    }
+#undef CDMF_G
+}
+
+}  // namespace
+
+struct cdmf_batch {
+    std::vector<cdmf_handle*> hs;
+    cudaStream_t s = nullptr;
+    int device = 0, rt = 0, T = 1, grid = 0, use_graph = 0;
+    uint32_t kmax = 0;
+    SweepArgs* d_desc = nullptr;
+    SweepArgs* h_desc = nullptr;     // pinned staging
+    size_t desc_cap = 0;
+    uint32_t* d_prefix = nullptr;
+    uint32_t* h_prefix = nullptr;
+    size_t prefix_cap = 0;
+    uint32_t* d_queue = nullptr;
+    size_t queue_cap = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int g_outer = -1;
+    std::vector<int> g_start;        // per problem: next_oiter, pending, p_for at capture
+    std::vector<int> g_end;
+    cdmf_stats g_single{};           // per-problem launches recorded while capturing
+    cdmf_stats st{};
+    std::string err;
+};
+
+namespace {
+
+int bfail(cdmf_batch* b, int code, const std::string& msg) {
+    if (b) b->err = msg;
+    return code;
+}
+
+#define BCU(b, call)                                                                            \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return bfail(b, CDMF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Host plan of n_outer lockstep outer iterations (state of the handles is
+// simulated and restored).
+void plan_batch(cdmf_batch* B, int n_outer, std::vector<BatchOp>& ops, std::vector<SweepArgs>& descs,
+                std::vector<uint32_t>& prefix) {
+    const int P = (int)B->hs.size();
+    struct Saved { int pending, p_for, next; };
+    std::vector<Saved> saved(P);
+    for (int q = 0; q < P; ++q) saved[q] = {B->hs[q]->pending, B->hs[q]->p_for, B->hs[q]->next_oiter};
+    uint32_t queues = 0;
+    for (int o = 0; o < n_outer; ++o) {
+        const int oiter = B->hs[0]->next_oiter;
+        for (int q = 0; q < P; ++q) {
+            cdmf_handle* h = B->hs[q];
+            if (h->rt != 0 && oiter > 1 && h->nnz > 0) {
+                ops.push_back({OP_REFRESH, q, 0, 0, false, false, 0, 0, 0, 0, 0, 0});
+                h->pending = -1;
+            }
+        }
+        for (uint32_t t = 0; t < B->kmax && B->T > 0; ++t) {
+            std::vector<int> part;
+            for (int q = 0; q < P; ++q)
+                if (t < B->hs[q]->o.k) part.push_back(q);
+            if (part.empty()) break;
+            const bool sub = B->hs[part[0]]->pending >= 0, add = oiter > 1;
+            for (int q : part)
+                if (B->hs[q]->p_for != (int)t) {
+                    ops.push_back({OP_PACK, q, t, 0, false, false, 0, 0, 0, 0, 0, 0});
+                    B->hs[q]->p_for = (int)t;
+                }
+            for (int it = 1; it <= B->T; ++it) {
+                const uint32_t off = (uint32_t)descs.size();
+                std::vector<SweepArgs> Bs;
+                std::vector<uint32_t> pa, pb;
+                uint32_t ca = 0, cb = 0;
+                for (int q : part) {
+                    SweepArgs A, Bq;
+                    feature_args(B->hs[q], t, it, A, Bq);
+                    descs.push_back(A);
+                    Bs.push_back(Bq);
+                    const DevBins& DA = B->hs[q]->csc;
+                    const DevBins& DB = B->hs[q]->csr;
+                    pa.push_back(ca);
+                    pb.push_back(cb);
+                    ca += DA.nx + DA.nc + DA.nwb + DA.ngb + DA.ntb;
+                    cb += DB.nx + DB.nc + DB.nwb + DB.ngb + DB.ntb;
+                }
+                pa.push_back(ca);
+                pb.push_back(cb);
+                const uint32_t offB = (uint32_t)descs.size();
+                descs.insert(descs.end(), Bs.begin(), Bs.end());
+                const uint32_t poA = (uint32_t)prefix.size();
+                prefix.insert(prefix.end(), pa.begin(), pa.end());
+                const uint32_t poB = (uint32_t)prefix.size();
+                prefix.insert(prefix.end(), pb.begin(), pb.end());
+                const int mA = it == 1 ? M_CSC : M_PLAIN, mB = it == 1 ? M_CSR : M_PLAIN;
+                ops.push_back({OP_GSWEEP, -1, t, mA, sub, add, K_CSC, off, (uint32_t)part.size(), poA, queues++, 0});
+                ops.push_back({OP_GSWEEP, -1, t, mB, sub, add, K_CSR, offB, (uint32_t)part.size(), poB, queues++, 0});
+            }
+            for (int q : part) {
+                ops.push_back({OP_FINISH, q, t, 0, false, false, 0, 0, 0, 0, 0, 0});
+                feature_finish(B->hs[q], t);
+            }
+        }
+        for (int q = 0; q < P; ++q) {
+            if (B->hs[q]->o.rmse_each_outer && B->hs[q]->nt > 0)
+                ops.push_back({OP_RMSE, q, 0, 0, false, false, 0, 0, 0, 0, 0, o});
+            B->hs[q]->next_oiter++;
+        }
+    }
+    for (int q = 0; q < P; ++q) {
+        B->hs[q]->pending = saved[q].pending;
+        B->hs[q]->p_for = saved[q].p_for;
+        B->hs[q]->next_oiter = saved[q].next;
+    }
+}
+
+template <class T>
+int grow_pair(cdmf_batch* B, T** d, T** hpin, size_t& cap, size_t need) {
+    if (need <= cap) return CDMF_OK;
+    if (*d) cudaFree(*d);
+    if (*hpin) cudaFreeHost(*hpin);
+    *d = nullptr;
+    *hpin = nullptr;
+    cap = 0;
+    if (cudaMalloc((void**)d, sizeof(T) * need) != cudaSuccess) return bfail(B, CDMF_ERR_ALLOC, "batch descriptors");
+    if (cudaHostAlloc((void**)hpin, sizeof(T) * need, cudaHostAllocDefault) != cudaSuccess)
+        return bfail(B, CDMF_ERR_ALLOC, "batch descriptors (host)");
+    cap = need;
+    return CDMF_OK;
+}
+
+int execute_batch(cdmf_batch* B, const std::vector<BatchOp>& ops, size_t ndesc, size_t nprefix, uint32_t nqueue) {
+    BCU(B, cudaMemcpyAsync(B->d_desc, B->h_desc, sizeof(SweepArgs) * ndesc, cudaMemcpyHostToDevice, B->s));
+    BCU(B, cudaMemcpyAsync(B->d_prefix, B->h_prefix, 4 * nprefix, cudaMemcpyHostToDevice, B->s));
+    BCU(B, cudaMemsetAsync(B->d_queue, 0, 4 * std::max<uint32_t>(1, nqueue), B->s));
+    for (const BatchOp& op : ops) {
+        int r = CDMF_OK;
+        switch (op.kind) {
+            case OP_PACK: r = feature_prepare(B->hs[op.q], op.t); break;
+            case OP_REFRESH: r = refresh_residual(B->hs[op.q]); break;
+            case OP_FINISH: feature_finish(B->hs[op.q], op.t); break;
+            case OP_RMSE: r = launch_rmse(B->hs[op.q], B->hs[op.q]->rmse_out + op.slot); break;
+            case OP_GSWEEP: {
+                const SweepArgs* d = B->d_desc + op.desc_off;
+                const uint32_t* pre = B->d_prefix + op.prefix_off;
+                uint32_t* qu = B->d_queue + op.queue;
+                switch (B->rt) {
+                    case 0: grouped_rt<0>(op.mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
+                    case 1: grouped_rt<1>(op.mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
+                    default: grouped_rt<2>(op.mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
+                }
+                BCU(B, cudaGetLastError());
+                B->st.launches++;
+                if (op.side == K_CSC) B->st.sweep_csc_launches++;
+                else B->st.sweep_csr_launches++;
+                break;
+            }
+        }
+        if (r) return bfail(B, r, B->hs[op.q >= 0 ? op.q : 0]->err);
+    }
+    return CDMF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void cdmf_cuda_batch_destroy(cdmf_batch* B) {
+    if (!B) return;
+    cudaSetDevice(B->device);
+    if (B->s) cudaStreamSynchronize(B->s);
+    for (cdmf_handle* h : B->hs) {
+        if (!h) continue;
+        h->s = nullptr;   // the batch stream is destroyed once, below
+        cdmf_cuda_destroy(h);
+    }
+    if (B->gexec) cudaGraphExecDestroy(B->gexec);
+    if (B->d_desc) cudaFree(B->d_desc);
+    if (B->h_desc) cudaFreeHost(B->h_desc);
+    if (B->d_prefix) cudaFree(B->d_prefix);
+    if (B->h_prefix) cudaFreeHost(B->h_prefix);
+    if (B->d_queue) cudaFree(B->d_queue);
+    if (B->e0) cudaEventDestroy(B->e0);
+    if (B->e1) cudaEventDestroy(B->e1);
+    if (B->s) cudaStreamDestroy(B->s);
+    delete B;
+}
+
+const char* cdmf_cuda_batch_last_error(const cdmf_batch* B) { return B ? B->err.c_str() : ""; }
+
+int cdmf_cuda_batch_create(const cdmf_problem* probs, const cdmf_opts* opts, int nprob, cdmf_batch** out) {
+    if (!out) return CDMF_ERR_INVALID;
+    *out = nullptr;
+    if (!probs || !opts || nprob <= 0) return CDMF_ERR_INVALID;
+    for (int q = 1; q < nprob; ++q)
+        if (opts[q].residual != opts[0].residual || opts[q].maxinneriter != opts[0].maxinneriter ||
+            opts[q].device != opts[0].device || opts[q].reduce != opts[0].reduce)
+            return CDMF_ERR_UNSUPPORTED;
+    cdmf_batch* B = new cdmf_batch();
+    B->device = opts[0].device;
+    B->rt = opts[0].residual;
+    B->T = opts[0].maxinneriter;
+    B->use_graph = opts[0].use_graph;
+    auto bail = [&](int code) { cdmf_cuda_batch_destroy(B); return code; };
+    if (cudaSetDevice(B->device) != cudaSuccess) return bail(CDMF_ERR_NO_DEVICE);
+    if (cudaStreamCreateWithFlags(&B->s, cudaStreamNonBlocking) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    if (cudaEventCreate(&B->e0) != cudaSuccess || cudaEventCreate(&B->e1) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    for (int q = 0; q < nprob; ++q) {
+        cdmf_opts o = opts[q];
+        o.version = 1;        // grouped sweeps use the binned kernel
+        o.use_graph = 0;
+        cdmf_handle* h = nullptr;
+        const int r = cdmf_cuda_create(probs + q, &o, &h);
+        if (r) return bail(r);
+        cudaStreamSynchronize(h->s);
+        cudaStreamDestroy(h->s);
+        h->s = B->s;
+        B->hs.push_back(h);
+        B->kmax = std::max(B->kmax, o.k);
+    }
+    int per_sm = 0, sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_sweep_kernel<0, M_CSR, true, true>, kBlock, 0);
+    B->grid = std::max(1, sms) * std::max(1, per_sm);
+    *out = B;
+    return CDMF_OK;
+}
+
+int cdmf_cuda_batch_set_factors(cdmf_batch* B, const float* const* W0) {
+    if (!B) return CDMF_ERR_INVALID;
+    for (size_t q = 0; q < B->hs.size(); ++q) {
+        const int r = cdmf_cuda_set_factors(B->hs[q], W0 ? W0[q] : nullptr, nullptr);
+        if (r) return bfail(B, r, B->hs[q]->err);
+    }
+    return CDMF_OK;
+}
+
+int cdmf_cuda_batch_run(cdmf_batch* B, int n_outer, double* rmse_out) {
+    if (!B || n_outer < 0) return CDMF_ERR_INVALID;
+    const int P = (int)B->hs.size();
+    for (cdmf_handle* h : B->hs)
+        if (n_outer > h->o.maxiter + 1) return bfail(B, CDMF_ERR_INVALID, "n_outer beyond the RMSE slots");
+    BCU(B, cudaSetDevice(B->device));
+    B->st = cdmf_stats{};
+    for (cdmf_handle* h : B->hs) {
+        h->st = cdmf_stats{};
+        h->refreshed = false;
+    }
+    std::vector<BatchOp> ops;
+    std::vector<SweepArgs> descs;
+    std::vector<uint32_t> prefix;
+    plan_batch(B, n_outer, ops, descs, prefix);
+    uint32_t nqueue = 0;
+    for (const BatchOp& op : ops)
+        if (op.kind == OP_GSWEEP) nqueue = std::max(nqueue, op.queue + 1);
+    std::vector<int> start(3 * P);
+    for (int q = 0; q < P; ++q) {
+        start[3 * q] = B->hs[q]->next_oiter;
+        start[3 * q + 1] = B->hs[q]->pending;
+        start[3 * q + 2] = B->hs[q]->p_for;
+    }
+    int r;
+    BCU(B, cudaEventRecord(B->e0, B->s));
+    const bool reuse = B->use_graph && B->gexec && B->g_outer == n_outer && B->g_start == start;
+    if (reuse) {
+        BCU(B, cudaGraphLaunch(B->gexec, B->s));
+        for (int q = 0; q < P; ++q) {
+            B->hs[q]->next_oiter = B->g_end[3 * q];
+            B->hs[q]->pending = B->g_end[3 * q + 1];
+            B->hs[q]->p_for = B->g_end[3 * q + 2];
+            if (B->hs[q]->rt != 0 && n_outer > 0) B->hs[q]->refreshed = true;
+        }
+        for (const BatchOp& op : ops)
+            if (op.kind == OP_GSWEEP) {
+                B->st.launches++;
+                if (op.side == K_CSC) B->st.sweep_csc_launches++;
+                else B->st.sweep_csr_launches++;
+            }
+        B->st.launches += B->g_single.launches;
+        B->st.rmse_launches += B->g_single.rmse_launches;
+        B->st.refresh_launches += B->g_single.refresh_launches;
+    } else {
+        if ((r = grow_pair(B, &B->d_desc, &B->h_desc, B->desc_cap, std::max<size_t>(1, descs.size())))) return r;
+        if ((r = grow_pair(B, &B->d_prefix, &B->h_prefix, B->prefix_cap, std::max<size_t>(1, prefix.size()))))
+            return r;
+        if (nqueue > B->queue_cap) {
+            if (B->d_queue) cudaFree(B->d_queue);
+            B->d_queue = nullptr;
+            B->queue_cap = 0;
+            if (cudaMalloc((void**)&B->d_queue, 4 * (size_t)nqueue) != cudaSuccess)
+                return bfail(B, CDMF_ERR_ALLOC, "batch queues");
+            B->queue_cap = nqueue;
+        }
+        if (!B->d_queue && cudaMalloc((void**)&B->d_queue, 4) != cudaSuccess)
+            return bfail(B, CDMF_ERR_ALLOC, "batch queues");
+        std::copy(descs.begin(), descs.end(), B->h_desc);
+        std::copy(prefix.begin(), prefix.end(), B->h_prefix);
+        if (B->use_graph) {
+            if (B->gexec) { cudaGraphExecDestroy(B->gexec); B->gexec = nullptr; }
+            BCU(B, cudaStreamBeginCapture(B->s, cudaStreamCaptureModeThreadLocal));
+            r = execute_batch(B, ops, descs.size(), prefix.size(), nqueue);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(B->s, &g);
+            if (r || e != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return r ? r : bfail(B, CDMF_ERR_CUDA, cudaGetErrorString(e));
+            }
+            const cudaError_t ei = cudaGraphInstantiate(&B->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) return bfail(B, CDMF_ERR_CUDA, cudaGetErrorString(ei));
+            B->g_outer = n_outer;
+            B->g_start = start;
+            B->g_single = cdmf_stats{};
+            for (cdmf_handle* h : B->hs) {
+                B->g_single.launches += h->st.launches;
+                B->g_single.rmse_launches += h->st.rmse_launches;
+                B->g_single.refresh_launches += h->st.refresh_launches;
+            }
+            B->g_end.assign(3 * P, 0);
+            for (int q = 0; q < P; ++q) {
+                B->hs[q]->next_oiter += n_outer;
+                B->g_end[3 * q] = B->hs[q]->next_oiter;
+                B->g_end[3 * q + 1] = B->hs[q]->pending;
+                B->g_end[3 * q + 2] = B->hs[q]->p_for;
+            }
+            BCU(B, cudaGraphLaunch(B->gexec, B->s));
+        } else {
+            if ((r = execute_batch(B, ops, descs.size(), prefix.size(), nqueue))) return r;
+            for (int q = 0; q < P; ++q) B->hs[q]->next_oiter += n_outer;
+        }
+    }
+    BCU(B, cudaEventRecord(B->e1, B->s));
+    BCU(B, cudaEventSynchronize(B->e1));
+    float ms = 0;
+    BCU(B, cudaEventElapsedTime(&ms, B->e0, B->e1));
+    B->st.train_ms = ms;
+    for (cdmf_handle* h : B->hs) {
+        B->st.launches += h->st.launches;
+        B->st.rmse_launches += h->st.rmse_launches;
+        B->st.refresh_launches += h->st.refresh_launches;
+        B->st.updates += (int64_t)h->o.k * n_outer;
+    }
+    if (rmse_out)
+        for (int q = 0; q < P; ++q) {
+            cdmf_handle* h = B->hs[q];
+            if (h->o.rmse_each_outer && h->nt > 0) {
+                BCU(B, cudaMemcpy(rmse_out + (size_t)q * n_outer, h->rmse_out, sizeof(double) * n_outer,
+                                  cudaMemcpyDeviceToHost));
+            } else {
+                for (int o = 0; o < n_outer; ++o) rmse_out[(size_t)q * n_outer + o] = -1.0;
+            }
+        }
+    return CDMF_OK;
+}
+
+int cdmf_cuda_batch_run_sequential(cdmf_batch* B, int n_outer, double* rmse_out, double* ms_out) {
+    if (!B || n_outer < 0) return CDMF_ERR_INVALID;
+    BCU(B, cudaSetDevice(B->device));
+    BCU(B, cudaEventRecord(B->e0, B->s));
+    std::vector<std::vector<double>> rm(B->hs.size());
+    for (size_t q = 0; q < B->hs.size(); ++q) {
+        cdmf_handle* h = B->hs[q];
+        const bool want = h->o.rmse_each_outer && h->nt > 0;
+        rm[q].assign(std::max(1, n_outer), -1.0);
+        const int r = cdmf_cuda_run(h, n_outer, want ? rm[q].data() : nullptr);
+        if (r) return bfail(B, r, h->err);
+    }
+    BCU(B, cudaEventRecord(B->e1, B->s));
+    BCU(B, cudaEventSynchronize(B->e1));
+    float ms = 0;
+    BCU(B, cudaEventElapsedTime(&ms, B->e0, B->e1));
+    if (ms_out) *ms_out = ms;
+    if (rmse_out)
+        for (size_t q = 0; q < B->hs.size(); ++q)
+            for (int o = 0; o < n_outer; ++o) rmse_out[q * n_outer + o] = rm[q][o];
+    return CDMF_OK;
+}
+
+int cdmf_cuda_batch_get_factors(cdmf_batch* B, float* const* W, float* const* H) {
+    if (!B) return CDMF_ERR_INVALID;
+    for (size_t q = 0; q < B->hs.size(); ++q) {
+        const int r = cdmf_cuda_get_factors(B->hs[q], W ? W[q] : nullptr, H ? H[q] : nullptr);
+        if (r) return bfail(B, r, B->hs[q]->err);
+    }
+    return CDMF_OK;
+}
+
+int cdmf_cuda_batch_stats(const cdmf_batch* B, cdmf_stats* s) {
+    if (!B || !s) return CDMF_ERR_INVALID;
+    *s = B->st;
+    return CDMF_OK;
 }
 
 }  // extern "C"

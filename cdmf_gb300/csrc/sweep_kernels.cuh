@@ -310,9 +310,9 @@ __device__ __forceinline__ void line_scalars(const SweepArgs& A, uint32_t j, flo
     dj = (ADD || MODE == M_CSC) ? A.d[j] : 0.0f;
 }
 
+// Work of block b of one sweep (b in [0, nx + nc + nwb + ngb + ntb)).
 template <int RT, int MODE, bool SUB, bool ADD>
-__global__ void CDMF_SWEEP_BOUNDS sweep_kernel(const SweepArgs A) {
-    uint32_t b = blockIdx.x;
+__device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
     if (b < A.nx) {                                        // split-line chunk
         const XTask T = A.xt[b];
         float bj, dj;
@@ -400,6 +400,35 @@ __global__ void CDMF_SWEEP_BOUNDS sweep_kernel(const SweepArgs A) {
     h.s = __fmul_rn(A.lambda, __uint2float_rn(len));         // h starts at lambda*nnz (src/cdmf_ref.cpp:8)
     for (uint32_t q = beg; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
     write_line<MODE>(A, j, __fdiv_rn(g.s, h.s), bj, dj);
+}
+
+template <int RT, int MODE, bool SUB, bool ADD>
+__global__ void CDMF_SWEEP_BOUNDS sweep_kernel(const SweepArgs A) {
+    sweep_block<RT, MODE, SUB, ADD>(A, blockIdx.x);
+}
+
+// Many problems' sweeps in one persistent launch: resident blocks pull block
+// indices from a device work queue (an atomic counter) over the concatenated
+// block ranges of all problems; prefix[q] is problem q's first block.
+template <int RT, int MODE, bool SUB, bool ADD>
+__global__ void CDMF_SWEEP_BOUNDS grouped_sweep_kernel(const SweepArgs* __restrict__ descs,
+                                                       const uint32_t* __restrict__ prefix, uint32_t nprob,
+                                                       uint32_t* queue) {
+    __shared__ uint32_t blk;
+    const uint32_t total = prefix[nprob];
+    for (;;) {
+        if (threadIdx.x == 0) blk = atomicAdd(queue, 1u);
+        __syncthreads();
+        const uint32_t b = blk;
+        __syncthreads();
+        if (b >= total) return;
+        uint32_t lo = 0, hi = nprob;                       // last q with prefix[q] <= b
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (prefix[mid] <= b) lo = mid; else hi = mid;
+        }
+        sweep_block<RT, MODE, SUB, ADD>(descs[lo], b - prefix[lo]);
+    }
 }
 
 // P[i] = (prev[i] or 0, cur[i]): the packed CSC table when no sweep has

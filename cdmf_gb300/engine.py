@@ -187,3 +187,71 @@ def cdmf_cuda(R, W, H, param, log=print):
     W[...] = Wc
     H[...] = Hc
     return lines
+
+
+class Batch:
+    """Many independent factorisations advanced together (include/cdmf_cuda.h,
+    cdmf_cuda_batch_*): problems[q] is a RatingMatrix, runs[q] a dict of
+    k / lambda_ (and optionally the other make_opts arguments)."""
+
+    def __init__(self, problems, runs, maxiter, maxinneriter=1, residual="f32", use_graph=True, **kw):
+        self.lib = _lib.load()
+        self.R = list(problems)
+        self.ks = [int(r["k"]) for r in runs]
+        n = len(self.R)
+        self._probs = (_lib.Problem * n)(*[_problem(R) for R in self.R])
+        self._opts = (_lib.Opts * n)(*[make_opts(r["k"], r["lambda_"], maxiter, maxinneriter, residual=residual,
+                                                 use_graph=use_graph, **kw) for r in runs])
+        h = ctypes.c_void_p()
+        st = self.lib.cdmf_cuda_batch_create(self._probs, self._opts, n, ctypes.byref(h))
+        check(st, "cdmf_cuda_batch_create")
+        self.h = h
+        self.maxiter = maxiter
+
+    def close(self):
+        if self.h:
+            self.lib.cdmf_cuda_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, where):
+        if st != 0:
+            msg = self.lib.cdmf_cuda_batch_last_error(self.h)
+            raise _lib.CdmfError(st, where, msg.decode() if msg else "")
+
+    def set_factors(self, W0s):
+        arrs = [np.ascontiguousarray(w, np.float32) for w in W0s]
+        ptrs = (ctypes.POINTER(ctypes.c_float) * len(arrs))(*[ptr(a, ctypes.c_float) for a in arrs])
+        self._check(self.lib.cdmf_cuda_batch_set_factors(self.h, ptrs), "cdmf_cuda_batch_set_factors")
+
+    def run(self, n_outer):
+        out = np.zeros((len(self.R), max(1, n_outer)), np.float64)
+        self._check(self.lib.cdmf_cuda_batch_run(self.h, int(n_outer), ptr(out, ctypes.c_double)),
+                    "cdmf_cuda_batch_run")
+        return out[:, :n_outer]
+
+    def run_sequential(self, n_outer):
+        out = np.zeros((len(self.R), max(1, n_outer)), np.float64)
+        ms = ctypes.c_double()
+        self._check(self.lib.cdmf_cuda_batch_run_sequential(self.h, int(n_outer), ptr(out, ctypes.c_double),
+                                                            ctypes.byref(ms)), "cdmf_cuda_batch_run_sequential")
+        return out[:, :n_outer], ms.value
+
+    def factors(self):
+        Ws = [np.empty((k, R.m), np.float32) for k, R in zip(self.ks, self.R)]
+        Hs = [np.empty((k, R.n), np.float32) for k, R in zip(self.ks, self.R)]
+        F = ctypes.POINTER(ctypes.c_float)
+        pw = (F * len(Ws))(*[ptr(a, ctypes.c_float) for a in Ws])
+        ph = (F * len(Hs))(*[ptr(a, ctypes.c_float) for a in Hs])
+        self._check(self.lib.cdmf_cuda_batch_get_factors(self.h, pw, ph), "cdmf_cuda_batch_get_factors")
+        return Ws, Hs
+
+    def stats(self):
+        s = _lib.Stats()
+        self._check(self.lib.cdmf_cuda_batch_stats(self.h, ctypes.byref(s)), "cdmf_cuda_batch_stats")
+        return {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
