@@ -40,22 +40,27 @@ def _run_parallel(cmds):
         raise RuntimeError("native build failed:\n" + msg)
 
 
-def build(verbose=False):
-    """Compiles every translation unit and links the library and the CLI."""
-    os.makedirs(OBJDIR, exist_ok=True)
-    os.makedirs(LIBDIR, exist_ok=True)
+def build(verbose=False, defines=(), lib_path=None, obj_dir=None, with_cli=True):
+    """Compiles every translation unit and links the library and the CLI.
+    `defines` (e.g. ["CDMF_CHUNKS=4"]) and `lib_path` build a variant of the
+    CUDA library elsewhere (used for tuning sweeps)."""
+    obj_dir = obj_dir or OBJDIR
+    lib = lib_path or LIB
+    os.makedirs(obj_dir, exist_ok=True)
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
     os.makedirs(BINDIR, exist_ok=True)
     cmds, objs = [], []
+    dflags = ["-D" + d for d in defines]
     for src in CU_SOURCES:
-        obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
-        cmds.append([NVCC] + NVFLAGS + ["-c", os.path.join(CSRC, src), "-o", obj])
+        obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
+        cmds.append([NVCC] + NVFLAGS + dflags + ["-c", os.path.join(CSRC, src), "-o", obj])
         objs.append(obj)
     for src in CXX_SOURCES:
-        obj = os.path.join(OBJDIR, os.path.basename(src) + ".o")
+        obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
         cmds.append(["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, src), "-o", obj])
         objs.append(obj)
     cli_objs = []
-    for src in CLI_SOURCES:
+    for src in (CLI_SOURCES if with_cli else []):
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):
             continue
@@ -66,10 +71,10 @@ def build(verbose=False):
         for c in cmds:
             print(" ".join(c), file=sys.stderr)
     _run_parallel(cmds)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     _run_parallel([[NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fopenmp", "-lgomp"]])
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if cli_objs:
         _run_parallel([["g++", "-o", CLI] + cli_objs + ["-L", LIBDIR, "-lcdmf_cuda", "-Wl,-rpath,$ORIGIN/../lib",
                                                          "-fopenmp"]])
-    return LIB
+    return lib

@@ -127,10 +127,11 @@ def load():
     global _LIB
     if _LIB is not None:
         return _LIB
-    if not os.path.exists(_build.LIB):
-        raise ImportError(f"{_build.LIB} is missing: build it with "
+    path = os.environ.get("CDMF_LIB", _build.LIB)
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with "
                           "`python -c 'import __graft_entry__ as g; g.build()'`")
-    lib = ctypes.CDLL(_build.LIB)
+    lib = ctypes.CDLL(path)
     for name, (res, args) in EXPORTS.items():
         fn = getattr(lib, name)
         fn.restype = res

@@ -207,8 +207,13 @@ __device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, 
 
 // Pass over [beg, end) by S cooperating threads (this one is `lane`): a scalar
 // head up to the first 4-aligned position (lanes 0..2), then 4-element vector
-// chunks (chunk c to lane c mod S, two chunks in flight per lane), then a
+// chunks (chunk c to lane c mod S, kChunks chunks in flight per lane), then a
 // scalar tail.  Each lane visits its elements in increasing order.
+#ifndef CDMF_CHUNKS
+#define CDMF_CHUNKS 2
+#endif
+constexpr int kChunks = CDMF_CHUNKS;   // 4-element vector chunks in flight per lane
+
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
                                         float dj, float& gs, float& hs) {
@@ -218,17 +223,17 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
     const uint32_t vend = vbeg + ((end - vbeg) & ~3u);
     if (lane < vbeg - beg) elem1<RT, MODE, SUB, ADD>(A, beg + lane, bj, dj, g, h);
     uint32_t q = vbeg + 4u * lane;
-    for (; q + 4u * S < vend; q += 8u * S) {
-        uint32_t iv[2][4];
-        float r[2][4];
+    for (; q + 4u * S * (kChunks - 1) < vend; q += 4u * S * kChunks) {
+        uint32_t iv[kChunks][4];
+        float r[kChunks][4];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < kChunks; ++u) {
             const uint4 v = __ldcs((const uint4*)(A.idx + q + 4u * S * u));
             iv[u][0] = v.x; iv[u][1] = v.y; iv[u][2] = v.z; iv[u][3] = v.w;
             Res<RT>::ld4(A.res, q + 4u * S * u, r[u]);
         }
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < kChunks; ++u) {
             float y[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -241,7 +246,7 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
             for (int e = 0; e < 4; ++e) accumulate(g, h, y[e], r[u][e]);
         }
     }
-    if (q < vend) {
+    for (; q < vend; q += 4u * S) {
         const uint4 v = __ldcs((const uint4*)(A.idx + q));
         const uint32_t iv[4] = {v.x, v.y, v.z, v.w};
         float r[4], y[4];
