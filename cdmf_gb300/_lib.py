@@ -39,8 +39,13 @@ class Opts(ctypes.Structure):
         ("maxinneriter", ctypes.c_int32), ("version", ctypes.c_int32), ("residual", ctypes.c_int32),
         ("reduce", ctypes.c_int32), ("rmse_each_outer", ctypes.c_int32), ("use_graph", ctypes.c_int32),
         ("threads_per_block", ctypes.c_int32), ("device", ctypes.c_int32), ("verbose", ctypes.c_int32),
-        ("relabel", ctypes.c_int32),
+        ("relabel", ctypes.c_int32), ("autotune", ctypes.c_int32),
     ]
+
+
+class BinCfg(ctypes.Structure):
+    _fields_ = [("thread_max", ctypes.c_uint32), ("group_max", ctypes.c_uint32), ("warp_max", ctypes.c_uint32),
+                ("cta_max", ctypes.c_uint32), ("chunk", ctypes.c_uint32)]
 
 
 class Stats(ctypes.Structure):
@@ -90,6 +95,9 @@ EXPORTS = {
     "cdmf_cuda_set_state": (ctypes.c_int, [ctypes.c_void_p, c_f32p, c_f32p, c_f32p, c_f32p, ctypes.c_int]),
     "cdmf_cuda_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "cdmf_cuda_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats)]),
+    "cdmf_cuda_get_bincfg": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BinCfg)]),
+    "cdmf_cuda_set_bincfg": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BinCfg)]),
+    "cdmf_cuda_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BinCfg), c_f64p]),
     "cdmf_cuda_host_alloc": (ctypes.c_void_p, [ctypes.c_uint64]),
     "cdmf_cuda_host_free": (None, [ctypes.c_void_p]),
     "cdmf_cuda_bins": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_i64p, c_i64p]),

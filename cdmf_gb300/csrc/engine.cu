@@ -27,6 +27,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -146,6 +149,10 @@ struct cdmf_handle {
     // degree relabelling: new id -> caller id, new position -> caller position
     bool relabeled = false;
     std::vector<uint32_t> row_old, col_old, csr_pos, csc_pos;
+    // host copies of the line pointers (engine numbering) and the bin plan
+    std::vector<uint32_t> hptr_r, hptr_c;
+    BinCfg cfg;
+    bool seq = false;
     // 16-bit residual modes: CSR->CSC position map, row-major factor copies
     uint32_t* to_csc = nullptr;
     float *Wrm = nullptr, *Hrm = nullptr;
@@ -244,6 +251,17 @@ int upload_bins(cdmf_handle* h, DevBins& D, Bins&& B) {
     D.host.g.clear(); D.host.g.shrink_to_fit();
     D.host.t.clear(); D.host.t.shrink_to_fit();
     return CDMF_OK;
+}
+
+void free_bins(cdmf_handle* h, DevBins& D) {
+    void* ps[] = {D.x, D.c, D.w, D.g, D.t, D.part, D.xcount};
+    for (void* p : ps) {
+        if (!p) continue;
+        cudaFree(p);
+        auto it = std::find(h->allocs.begin(), h->allocs.end(), p);
+        if (it != h->allocs.end()) h->allocs.erase(it);
+    }
+    D = DevBins();
 }
 
 int upload_tiles(cdmf_handle* h, DevTiles& D, const uint32_t* ptr, int64_t lines, int64_t nnz) {
@@ -656,6 +674,55 @@ int do_outer_graph(cdmf_handle* h, int oiter, double* rmse_dst) {
     return CDMF_OK;
 }
 
+int replan(cdmf_handle* h, const BinCfg& cfg) {
+    free_bins(h, h->csr);
+    free_bins(h, h->csc);
+    h->cfg = cfg;
+    int r;
+    if ((r = upload_bins(h, h->csr, plan_bins(h->hptr_r.data(), h->m, h->seq, cfg))) ||
+        (r = upload_bins(h, h->csc, plan_bins(h->hptr_c.data(), h->n, h->seq, cfg))))
+        return r;
+    return CDMF_OK;
+}
+
+// Time of one steady-state feature (CSC + CSR sweep with subtract and
+// add-back) under the current bins, in ms; the state is scratch.
+int time_feature(cdmf_handle* h, int reps, double* ms) {
+    h->pending = 0;
+    h->p_for = 0;
+    SweepArgs A, B;
+    feature_args(h, 0, 1, A, B);
+    int r;
+    for (int w = 0; w < 1 + reps; ++w) {
+        if (w == 1) CU(h, cudaEventRecord(h->ev_start, h->s));
+        if ((r = launch_sweep(h, K_CSC, h->csc, A, M_CSC, true, true)) ||
+            (r = launch_sweep(h, K_CSR, h->csr, B, M_CSR, true, true)))
+            return r;
+    }
+    CU(h, cudaEventRecord(h->ev_stop, h->s));
+    CU(h, cudaEventSynchronize(h->ev_stop));
+    float t = 0;
+    CU(h, cudaEventElapsedTime(&t, h->ev_start, h->ev_stop));
+    *ms = t / reps;
+    return CDMF_OK;
+}
+
+struct TuneKey {
+    int64_t m, n, nnz;
+    int rt, relabeled;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(m, n, nnz, rt, relabeled) < std::tie(o.m, o.n, o.nnz, o.rt, o.relabeled);
+    }
+};
+std::map<TuneKey, BinCfg>& tune_cache() {
+    static std::map<TuneKey, BinCfg> c;
+    return c;
+}
+std::mutex& tune_mutex() {
+    static std::mutex mu;
+    return mu;
+}
+
 }  // namespace
 
 extern "C" {
@@ -826,9 +893,11 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
             return bail(CDMF_ERR_CUDA);
     }
     const bool seq = o->reduce == CDMF_REDUCE_SEQUENTIAL;
-    BinCfg cfg;
-    if ((r = upload_bins(h, h->csr, plan_bins(p->csr_row_ptr, m, seq, cfg))) ||
-        (r = upload_bins(h, h->csc, plan_bins(p->csc_col_ptr, n, seq, cfg))))
+    h->seq = seq;
+    h->hptr_r.assign(p->csr_row_ptr, p->csr_row_ptr + m + 1);
+    h->hptr_c.assign(p->csc_col_ptr, p->csc_col_ptr + n + 1);
+    if ((r = upload_bins(h, h->csr, plan_bins(p->csr_row_ptr, m, seq, h->cfg))) ||
+        (r = upload_bins(h, h->csc, plan_bins(p->csc_col_ptr, n, seq, h->cfg))))
         return bail(r);
     h->tiles = o->version == 3 && !seq;
     if (h->tiles && ((r = upload_tiles(h, h->tcsr, p->csr_row_ptr, m, N)) ||
@@ -841,6 +910,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if ((r = reset_residual(h, h->res_csr, h->csr_val)) || (r = reset_residual(h, h->res_csc, h->csc_val)))
         return bail(r);
     if (cudaStreamSynchronize(h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    if (o->autotune && (r = cdmf_cuda_autotune(h, nullptr, nullptr))) return bail(r);
     const double T = std::max(1, o->maxinneriter);
     const double br = (double)h->rbytes;
     h->st.bytes_per_update = T * 2.0 * N * (4.0 + br) + 2.0 * N * br + T * 4.0 * (m + n + 2) + 8.0 * (m + n);
@@ -1066,6 +1136,89 @@ int cdmf_cuda_bins(const cdmf_handle* h, int which, int64_t counts[5], int64_t n
         if (counts) counts[q] = B.count[q];
         if (nnz) nnz[q] = B.nnz[q];
     }
+    return CDMF_OK;
+}
+
+int cdmf_cuda_get_bincfg(const cdmf_handle* h, cdmf_bincfg* c) {
+    if (!h || !c) return CDMF_ERR_INVALID;
+    c->thread_max = h->cfg.thread_max;
+    c->group_max = h->cfg.group_max;
+    c->warp_max = h->cfg.warp_max;
+    c->cta_max = h->cfg.cta_max;
+    c->chunk = h->cfg.chunk;
+    return CDMF_OK;
+}
+
+int cdmf_cuda_set_bincfg(cdmf_handle* h, const cdmf_bincfg* c) {
+    if (!h || !c) return CDMF_ERR_INVALID;
+    if (c->chunk < 256 || c->chunk % 4 || c->thread_max > c->warp_max || c->warp_max > c->cta_max ||
+        c->cta_max < c->chunk || (c->group_max && (c->group_max < c->thread_max || c->group_max > c->warp_max)))
+        return fail(h, CDMF_ERR_INVALID, "inconsistent bin thresholds");
+    CU(h, cudaSetDevice(h->o.device));
+    BinCfg cfg;
+    cfg.thread_max = c->thread_max;
+    cfg.group_max = c->group_max ? c->group_max : c->thread_max;
+    cfg.warp_max = c->warp_max;
+    cfg.cta_max = c->cta_max;
+    cfg.chunk = c->chunk;
+    return replan(h, cfg);
+}
+
+int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms) {
+    if (!h) return CDMF_ERR_INVALID;
+    CU(h, cudaSetDevice(h->o.device));
+    if (h->seq || h->tiles || h->nnz == 0 || h->o.maxinneriter <= 0) {
+        if (chosen) cdmf_cuda_get_bincfg(h, chosen);
+        if (best_ms) *best_ms = 0;
+        return CDMF_OK;
+    }
+    const TuneKey key{h->m, h->n, h->nnz, h->rt, h->relabeled ? 1 : 0};
+    int r;
+    BinCfg best = h->cfg;
+    double best_t = 0;
+    bool cached = false;
+    {
+        std::lock_guard<std::mutex> lk(tune_mutex());
+        auto it = tune_cache().find(key);
+        if (it != tune_cache().end()) { best = it->second; cached = true; }
+    }
+    if (!cached) {
+        const bool prof = h->profiling;
+        h->profiling = false;
+        // coordinate search over group_max, warp_max, cta_max
+        if ((r = time_feature(h, 3, &best_t))) return r;
+        const uint32_t gvals[] = {0, 64, 128, 256, 512};
+        const uint32_t wvals[] = {1024, 2048, 4096};
+        const uint32_t cvals[] = {8192, 16384, 65536};
+        for (int dim = 0; dim < 3; ++dim) {
+            const uint32_t* vals = dim == 0 ? gvals : dim == 1 ? wvals : cvals;
+            const int nv = dim == 0 ? 5 : 3;
+            BinCfg base = best;
+            for (int v = 0; v < nv; ++v) {
+                BinCfg c = base;
+                if (dim == 0) c.group_max = vals[v] ? vals[v] : c.thread_max;
+                if (dim == 1) c.warp_max = vals[v];
+                if (dim == 2) c.cta_max = vals[v];
+                if (c.group_max > c.warp_max || c.warp_max > c.cta_max) continue;
+                if (c.group_max == best.group_max && c.warp_max == best.warp_max && c.cta_max == best.cta_max) continue;
+                if ((r = replan(h, c))) return r;
+                double t = 0;
+                if ((r = time_feature(h, 3, &t))) return r;
+                if (t < best_t) { best_t = t; best = c; }
+            }
+        }
+        h->profiling = prof;
+        std::lock_guard<std::mutex> lk(tune_mutex());
+        tune_cache()[key] = best;
+    }
+    if ((r = replan(h, best))) return r;
+    // the timing sweeps used the factors and residual as scratch
+    if ((r = cdmf_cuda_set_factors(h, nullptr, nullptr))) return r;
+    CU(h, cudaMemsetAsync(h->P, 0, sizeof(float2) * std::max<int64_t>(1, h->m), h->s));
+    CU(h, cudaMemsetAsync(h->Q, 0, sizeof(float4) * std::max<int64_t>(1, h->n), h->s));
+    CU(h, cudaStreamSynchronize(h->s));
+    if (chosen) cdmf_cuda_get_bincfg(h, chosen);
+    if (best_ms) *best_ms = best_t;
     return CDMF_OK;
 }
 

@@ -46,7 +46,8 @@ def _problem(R):
 
 
 def make_opts(k, lambda_, maxiter=5, maxinneriter=5, version=1, residual="f32", reduce="tree",
-              rmse_each_outer=True, use_graph=False, device=0, threads_per_block=0, verbose=0, relabel=True):
+              rmse_each_outer=True, use_graph=False, device=0, threads_per_block=0, verbose=0, relabel=True,
+              autotune=False):
     o = _lib.Opts()
     _lib.load().cdmf_opts_default(ctypes.byref(o))
     o.k, o.lambda_, o.maxiter, o.maxinneriter = int(k), float(lambda_), int(maxiter), int(maxinneriter)
@@ -57,6 +58,7 @@ def make_opts(k, lambda_, maxiter=5, maxinneriter=5, version=1, residual="f32", 
     o.use_graph = int(bool(use_graph))
     o.device, o.threads_per_block, o.verbose = int(device), int(threads_per_block), int(verbose)
     o.relabel = int(bool(relabel))
+    o.autotune = int(bool(autotune))
     return o
 
 
@@ -141,6 +143,21 @@ class Engine:
         s = _lib.Stats()
         check(self.lib.cdmf_cuda_stats(self.h, ctypes.byref(s)), "cdmf_cuda_stats", self.h)
         return {f: getattr(s, f) for f, _ in _lib.Stats._fields_}
+
+    def bincfg(self):
+        c = _lib.BinCfg()
+        check(self.lib.cdmf_cuda_get_bincfg(self.h, ctypes.byref(c)), "cdmf_cuda_get_bincfg", self.h)
+        return {f: getattr(c, f) for f, _ in _lib.BinCfg._fields_}
+
+    def set_bincfg(self, **kw):
+        c = _lib.BinCfg(**{**self.bincfg(), **kw})
+        check(self.lib.cdmf_cuda_set_bincfg(self.h, ctypes.byref(c)), "cdmf_cuda_set_bincfg", self.h)
+
+    def autotune(self):
+        c = _lib.BinCfg()
+        ms = ctypes.c_double()
+        check(self.lib.cdmf_cuda_autotune(self.h, ctypes.byref(c), ctypes.byref(ms)), "cdmf_cuda_autotune", self.h)
+        return {f: getattr(c, f) for f, _ in _lib.BinCfg._fields_}, ms.value
 
     def bins(self, which):
         """which: 'csr' or 'csc' -> (lines per bin, nnz per bin) for (thread, group8, warp, cta, split)."""

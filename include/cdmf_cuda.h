@@ -89,7 +89,16 @@ typedef struct {
     int32_t verbose;
     int32_t relabel;          /* 1: renumber rows and columns by degree inside the engine
                                  (tree order only; results come back in the caller's numbering) */
+    int32_t autotune;         /* 1: pick the bin thresholds by timing candidates on this matrix
+                                 at create (cached per matrix shape in the process) */
 } cdmf_opts;
+
+/* Line-length bin thresholds of the binned sweeps (versions 1/2), in
+ * nonzeros: <= thread_max one thread per line, <= group_max 8 lanes,
+ * <= warp_max a warp, <= cta_max a CTA, above: split in chunks of `chunk`. */
+typedef struct {
+    uint32_t thread_max, group_max, warp_max, cta_max, chunk;
+} cdmf_bincfg;
 
 /* Engine timings and counters of the most recent cdmf_cuda_run/train. */
 typedef struct {
@@ -151,6 +160,13 @@ int cdmf_cuda_set_state(cdmf_handle* h, const float* W, const float* H, const fl
                         const float* res_csr, int next_oiter);
 int cdmf_cuda_set_profiling(cdmf_handle* h, int on);
 int cdmf_cuda_stats(const cdmf_handle* h, cdmf_stats* s);
+/* Bin thresholds: read, set (re-plans the bins), or pick by timing one
+ * steady-state feature per candidate on this matrix (coordinate search over
+ * group_max, warp_max, cta_max).  Autotuning uses the factors and residual
+ * as scratch and leaves a fresh state (as cdmf_cuda_set_factors(h, NULL, NULL)). */
+int cdmf_cuda_get_bincfg(const cdmf_handle* h, cdmf_bincfg* c);
+int cdmf_cuda_set_bincfg(cdmf_handle* h, const cdmf_bincfg* c);
+int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms);
 /* Page-locked host memory for inputs and outputs of cdmf_cuda_train /
  * create / get_factors (copies from it run at full link speed).  NULL on
  * failure. */

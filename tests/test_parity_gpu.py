@@ -322,3 +322,25 @@ def test_tile_version_deterministic():
             outs.append(e.state())
     for f in ("W", "H", "res_csc", "res_csr"):
         assert np.array_equal(bits(outs[0][f]), bits(outs[1][f])), f
+
+
+def test_autotune_and_bincfg(cpu_scale):
+    """The autotuner picks valid thresholds, leaves a fresh state, and any
+    bin plan keeps the results within the FP32 budget."""
+    R, run, W0, ref = cpu_scale
+    with engine.Engine(R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"]) as e:
+        cfg, ms = e.autotune()
+        assert ms > 0 and cfg["thread_max"] <= cfg["warp_max"] <= cfg["cta_max"]
+        assert e.bincfg() == cfg
+        for plan in (cfg, dict(group_max=0, warp_max=1024, cta_max=8192)):
+            e.set_bincfg(**plan)
+            e.set_factors(W0)
+            rm = e.run(run["maxiter"])
+            W, H = e.factors()
+            okw, gw = within_budget(W, ref["W"], ref["f64"]["W"])
+            okh, gh = within_budget(H, ref["H"], ref["f64"]["H"])
+            assert okw and okh, (plan, gw, gh)
+            assert all(rmse_ok(a, b, c) for a, b, c in zip(rm, ref["rmse"], ref["f64"]["rmse"]))
+    with pytest.raises(Exception):
+        with engine.Engine(R, run["k"], run["lambda_"], 1, 1) as e:
+            e.set_bincfg(warp_max=100, cta_max=50)
