@@ -17,7 +17,7 @@
 // the packed table Q; the CSR sweep overwrites W[t] in place (each row reads
 // only its own old w_i before writing it) and writes the packed table P the
 // next feature's CSC sweep gathers from.
-#include "../../include/cdmf_cuda.h"
+#include <cdmf_cuda.h>
 #include "sweep_kernels.cuh"
 #include "refresh_kernels.cuh"
 #include "tile_kernels.cuh"

@@ -1,6 +1,6 @@
 // Degree relabelling of a cdmf_problem (see relabel.cpp).
 #pragma once
-#include "../../include/cdmf_cuda.h"
+#include <cdmf_cuda.h>
 
 #include <cstdint>
 #include <vector>

@@ -15,8 +15,8 @@
 //      quantum and clamped;
 //   6. a uniform hold-out of nnz_test entries (the smallest hash keys), the
 //      rest compacted into the train CSR, and CSC by a stable counting sort.
-#include "../../include/cdmf_synth.h"
-#include "../../include/cdmf_cuda.h"
+#include <cdmf_synth.h>
+#include <cdmf_cuda.h>
 
 #include <algorithm>
 #include <cmath>

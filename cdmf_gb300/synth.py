@@ -112,7 +112,7 @@ def batch_specs(count=64, seed=0):
         nnz = min(nnz, int(0.3 * m * n))
         k = int(rng.choice([8, 16, 32]))
         lam = float(rng.choice([0.01, 0.05, 0.1, 0.5]))
-        matrix = dict(m=m, n=n, nnz_total=nnz, test_fraction=0.01, row_alpha=0.9, row_min=1,
+        matrix = dict(m=m, n=n, nnz_total=nnz, test_fraction=0.01, row_alpha=0.9, row_min=1 if nnz >= 2 * m else 0,
                       row_max=max(1, n // 2), col_alpha=0.9, col_cap=max(1, m // 2), rank=8, factor_std=0.6,
                       offset=3.0, noise_std=0.5, quantum=1.0, vmin=1.0, vmax=5.0, seed=seed * 1000 + p)
         out.append(dict(matrix=matrix, run=dict(k=k, lambda_=lam, maxiter=10, maxinneriter=1)))
