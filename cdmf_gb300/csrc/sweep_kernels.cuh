@@ -21,10 +21,12 @@
 // The CSC sweep writes Q as it finishes each column; the last CSR sweep of a
 // feature writes P for the next feature as it finishes each row.
 //
-// Streams.  Inside a line, index and residual are read with 128-bit (16-bit
-// residual: 64-bit) vector loads, 4 nonzeros per lane per load, after a
-// scalar head that reaches a 4-element boundary; cache-streaming hints keep
-// them out of L1, which holds the gather tables.
+// Streams.  Inside a line the lanes of a warp take consecutive nonzeros, so
+// both the coalesced index/residual loads and the gathers that follow cover
+// neighbouring positions (the gathered cross indices of a sorted line are
+// close together, few cache lines per gather); each lane keeps kIlp
+// nonzeros in flight.  Cache-streaming hints keep the streams out of L1,
+// which holds the gather tables.
 //
 // Lines are binned by length and all bins run in the same launch:
 //   blocks [0, nx)            one chunk of a split line (len > cta_max); the
@@ -212,8 +214,15 @@ __device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, 
 #ifndef CDMF_CHUNKS
 #define CDMF_CHUNKS 2
 #endif
-constexpr int kChunks = CDMF_CHUNKS;   // 4-element vector chunks in flight per lane
+#ifndef CDMF_ILP
+#define CDMF_ILP 8
+#endif
+constexpr int kChunks = CDMF_CHUNKS;   // vector layout: 4-element chunks in flight per lane
+constexpr int kIlp = CDMF_ILP;         // interleaved layout: elements in flight per lane
 
+#ifdef CDMF_VEC_STREAMS
+// Vector layout: lane takes 4 consecutive nonzeros per 128-bit load, after a
+// scalar head that reaches a 4-aligned position, then a scalar tail.
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
                                         float dj, float& gs, float& hs) {
@@ -265,6 +274,37 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
     gs = g.value();
     hs = h.value();
 }
+#else
+// Interleaved layout: lane takes nonzeros beg+lane, beg+lane+S, ... so that
+// the S lanes of one load, and of the gather that follows it, touch S
+// consecutive nonzeros -- neighbouring cross indices, few cache lines per
+// gather.  kIlp nonzeros per lane are in flight per step.
+template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
+__device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
+                                        float dj, float& gs, float& hs) {
+    Acc<KAHAN> g, h;
+    uint32_t q = beg + lane;
+    for (; q + (uint32_t)S * (kIlp - 1) < end; q += (uint32_t)S * kIlp) {
+        uint32_t iv[kIlp];
+        float r[kIlp], a[kIlp], c[kIlp], y[kIlp];
+#pragma unroll
+        for (int u = 0; u < kIlp; ++u) {
+            iv[u] = __ldcs(A.idx + q + S * u);
+            r[u] = Res<RT>::ld(A.res, q + S * u);
+        }
+#pragma unroll
+        for (int u = 0; u < kIlp; ++u) fetch<MODE>(A, iv[u], a[u], c[u], y[u]);
+#pragma unroll
+        for (int u = 0; u < kIlp; ++u) {
+            if (SUB || ADD) r[u] = Res<RT>::st(A.res, q + S * u, update<SUB, ADD>(r[u], a[u], c[u], bj, dj));
+            accumulate(g, h, y[u], r[u]);
+        }
+    }
+    for (; q < end; q += S) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
+    gs = g.value();
+    hs = h.value();
+}
+#endif
 
 template <int WIDTH = 32>
 __device__ __forceinline__ void warp_sum2(float& g, float& h) {
