@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <set>
 #include <mutex>
 #include <tuple>
 #include <cstdio>
@@ -324,8 +325,23 @@ struct Timed {
     }
 };
 
+// The sweeps use almost no shared memory; give the unified L1/shared
+// storage to L1, which holds the gather tables.
+template <class K>
+void prefer_l1(K kernel) {
+    static std::mutex mu;
+    static std::set<const void*> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.insert((const void*)kernel).second)
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+}
+
 template <int RT, int MODE>
 void launch_mode(const SweepArgs& A, bool sub, bool add, unsigned grid, cudaStream_t s) {
+    prefer_l1(sweep_kernel<RT, MODE, true, true>);
+    prefer_l1(sweep_kernel<RT, MODE, true, false>);
+    prefer_l1(sweep_kernel<RT, MODE, false, true>);
+    prefer_l1(sweep_kernel<RT, MODE, false, false>);
     if (MODE == M_PLAIN) sweep_kernel<RT, M_PLAIN, false, false><<<grid, kBlock, 0, s>>>(A);
     else if (sub && add) sweep_kernel<RT, MODE, true, true><<<grid, kBlock, 0, s>>>(A);
     else if (sub) sweep_kernel<RT, MODE, true, false><<<grid, kBlock, 0, s>>>(A);
@@ -342,6 +358,10 @@ void launch_rt(const SweepArgs& A, int mode, bool sub, bool add, unsigned grid, 
 
 template <int RT, int MODE>
 void tile_mode(const TileArgs& T, bool sub, bool add, unsigned grid, cudaStream_t s) {
+    prefer_l1(tile_sweep_kernel<RT, MODE, true, true>);
+    prefer_l1(tile_sweep_kernel<RT, MODE, true, false>);
+    prefer_l1(tile_sweep_kernel<RT, MODE, false, true>);
+    prefer_l1(tile_sweep_kernel<RT, MODE, false, false>);
     if (MODE == M_PLAIN) tile_sweep_kernel<RT, M_PLAIN, false, false><<<grid, kBlock, 0, s>>>(T);
     else if (sub && add) tile_sweep_kernel<RT, MODE, true, true><<<grid, kBlock, 0, s>>>(T);
     else if (sub) tile_sweep_kernel<RT, MODE, true, false><<<grid, kBlock, 0, s>>>(T);
@@ -1324,6 +1344,13 @@ struct BatchOp {
 template <int RT>
 void grouped_rt(int mode, bool sub, bool add, const SweepArgs* d, const uint32_t* pre, uint32_t nq, uint32_t* queue,
                 int grid, cudaStream_t s) {
+    prefer_l1(grouped_sweep_kernel<RT, M_CSC, true, true>);
+    prefer_l1(grouped_sweep_kernel<RT, M_CSR, true, true>);
+    prefer_l1(grouped_sweep_kernel<RT, M_CSC, true, false>);
+    prefer_l1(grouped_sweep_kernel<RT, M_CSR, true, false>);
+    prefer_l1(grouped_sweep_kernel<RT, M_CSC, false, true>);
+    prefer_l1(grouped_sweep_kernel<RT, M_CSR, false, true>);
+    prefer_l1(grouped_sweep_kernel<RT, M_PLAIN, false, false>);
 #define CDMF_G(M, S, A) grouped_sweep_kernel<RT, M, S, A><<<grid, kBlock, 0, s>>>(d, pre, nq, queue)
     if (mode == M_PLAIN) CDMF_G(M_PLAIN, false, false);
     else if (mode == M_CSC) {

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kBlock) refresh_kernel(
     const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ idx, const float* __restrict__ val,
     const uint32_t* __restrict__ to_csc, int64_t m, int64_t nnz, const float* __restrict__ Wrm,
     const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr, void* __restrict__ res_csc,
-    const float* __restrict__ pa, const float* __restrict__ pb,   // pending subtract: a = H[tp] (cols), b = W[tp] (rows)
+    const float* __restrict__ pa, const float* __restrict__ pb_,  // pending subtract: a = H[tp] (cols), b = W[tp] (rows)
     double* part, uint32_t* counter, double* drift_out, unsigned long long* nonfinite_out) {
     __shared__ uint32_t srow[2];
     double drift = 0.0;
@@ -68,15 +68,24 @@ __global__ void __launch_bounds__(kBlock) refresh_kernel(
         }
         __syncthreads();
         const uint32_t rlo = srow[0], rhi = srow[1];
-        for (int u = 0; u < kRefreshPerThread; ++u) {
-            const int64_t p = p0 + threadIdx.x + (int64_t)u * kBlock;
-            if (p >= p1) break;
+        // each thread takes kRefreshPerThread consecutive nonzeros: one
+        // binary search for the first, then the row advances by walking
+        const int64_t pb = p0 + (int64_t)threadIdx.x * kRefreshPerThread;
+        uint32_t i = rlo, bound = 0;
+        if (pb < p1) {
             uint32_t lo = rlo, hi = rhi + 1;
             while (hi - lo > 1) {
                 const uint32_t mid = (lo + hi) >> 1;
-                if ((int64_t)__ldg(ptr + mid) <= p) lo = mid; else hi = mid;
+                if ((int64_t)__ldg(ptr + mid) <= pb) lo = mid; else hi = mid;
             }
-            const uint32_t i = lo, j = __ldcs(idx + p);
+            i = lo;
+            bound = __ldg(ptr + i + 1);
+        }
+        for (int u = 0; u < kRefreshPerThread; ++u) {
+            const int64_t p = pb + u;
+            if (p >= p1) break;
+            while ((uint32_t)p >= bound) bound = __ldg(ptr + (++i) + 1);
+            const uint32_t j = __ldg(idx + p);
             const float4* wr = (const float4*)(Wrm + (size_t)i * kp);
             const float4* hr = (const float4*)(Hrm + (size_t)j * kp);
             float dot = 0.0f;
@@ -87,11 +96,11 @@ __global__ void __launch_bounds__(kBlock) refresh_kernel(
                 dot = fmaf(w.z, h.z, dot);
                 dot = fmaf(w.w, h.w, dot);
             }
-            const float rnew = __fsub_rn(__ldcs(val + p), dot);
+            const float rnew = __fsub_rn(__ldg(val + p), dot);
             float rold = Res<RT>::ld(res_csr, (uint32_t)p);
-            if (pa) rold = __fsub_rn(rold, __fmul_rn(__ldg(pa + j), __ldg(pb + i)));
+            if (pa) rold = __fsub_rn(rold, __fmul_rn(__ldg(pa + j), __ldg(pb_ + i)));
             const float stored = Res<RT>::st(res_csr, (uint32_t)p, rnew);
-            Res<RT>::st(res_csc, __ldcs(to_csc + p), rnew);
+            Res<RT>::st(res_csc, __ldg(to_csc + p), rnew);
             if (!isfinite(stored)) bad++;
             const double d = (double)rnew - (double)rold;
             drift = __dadd_rn(drift, __dmul_rn(d, d));

@@ -21,12 +21,10 @@
 // The CSC sweep writes Q as it finishes each column; the last CSR sweep of a
 // feature writes P for the next feature as it finishes each row.
 //
-// Streams.  Inside a line the lanes of a warp take consecutive nonzeros, so
-// both the coalesced index/residual loads and the gathers that follow cover
-// neighbouring positions (the gathered cross indices of a sorted line are
-// close together, few cache lines per gather); each lane keeps kIlp
-// nonzeros in flight.  Cache-streaming hints keep the streams out of L1,
-// which holds the gather tables.
+// Streams.  Inside a line, index and residual are read with 128-bit (16-bit
+// residual: 64-bit) vector loads, 4 nonzeros per lane per load, after a
+// scalar head that reaches a 4-element boundary; cache-streaming hints keep
+// them out of L1, which holds the gather tables.
 //
 // Lines are binned by length and all bins run in the same launch:
 //   blocks [0, nx)            one chunk of a split line (len > cta_max); the
@@ -45,9 +43,13 @@ namespace cdmf {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
-// Minimum resident blocks per SM asked of the compiler (register cap).
-// Without a value the compiler picks freely.
-#ifdef CDMF_SWEEP_MIN_BLOCKS
+// Minimum resident blocks per SM asked of the compiler (register cap):
+// 6 blocks of 256 threads (at most 40 registers) measured best on the
+// 480,189 x 17,770 workload; 0 lets the compiler pick freely.
+#ifndef CDMF_SWEEP_MIN_BLOCKS
+#define CDMF_SWEEP_MIN_BLOCKS 6
+#endif
+#if CDMF_SWEEP_MIN_BLOCKS > 0
 #define CDMF_SWEEP_BOUNDS __launch_bounds__(kBlock, CDMF_SWEEP_MIN_BLOCKS)
 #else
 #define CDMF_SWEEP_BOUNDS __launch_bounds__(kBlock)
@@ -220,8 +222,8 @@ __device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, 
 constexpr int kChunks = CDMF_CHUNKS;   // vector layout: 4-element chunks in flight per lane
 constexpr int kIlp = CDMF_ILP;         // interleaved layout: elements in flight per lane
 
-#ifdef CDMF_VEC_STREAMS
-// Vector layout: lane takes 4 consecutive nonzeros per 128-bit load, after a
+#ifndef CDMF_INTERLEAVED_STREAMS
+// Vector layout (default; measured faster for 16-bit residuals): lane takes 4 consecutive nonzeros per 128-bit load, after a
 // scalar head that reaches a 4-aligned position, then a scalar tail.
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
@@ -275,7 +277,7 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
     hs = h.value();
 }
 #else
-// Interleaved layout: lane takes nonzeros beg+lane, beg+lane+S, ... so that
+// Interleaved layout (CDMF_INTERLEAVED_STREAMS): lane takes nonzeros beg+lane, beg+lane+S, ... so that
 // the S lanes of one load, and of the gather that follows it, touch S
 // consecutive nonzeros -- neighbouring cross indices, few cache lines per
 // gather.  kIlp nonzeros per lane are in flight per step.
