@@ -166,12 +166,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
-    ap.add_argument("--residual", default="f32", choices=["f32", "bf16", "f16"])
+    ap.add_argument("--residual", default="bf16", choices=["f32", "bf16", "f16"],
+                    help="residual storage of the headline run (mixed precision: bf16)")
+    ap.add_argument("--compare", default="f32", choices=["f32", "bf16", "f16", "none"],
+                    help="residual storage of the comparison run reported beside the headline")
     ap.add_argument("--k", type=int, default=64)
-    ap.add_argument("--version", type=int, default=3, choices=[1, 2, 3],
+    ap.add_argument("--version", type=int, default=1, choices=[1, 2, 3],
                     help="1/2: row-length-binned sweeps, 3: nonzero-balanced tiles")
     ap.add_argument("--graph", type=int, default=1, help="replay outer iterations from CUDA graphs")
     ap.add_argument("--relabel", type=int, default=1, help="renumber rows and columns by degree inside the engine")
+    ap.add_argument("--layout", default="lines", choices=["lines", "blocked"],
+                    help="residual copy layout: lines (binned sweeps) or blocked (shared-memory gather tables)")
     ap.add_argument("--e2e-outer", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -226,37 +231,44 @@ def main():
     k, lam, T = run["k"], run["lambda_"], run["maxinneriter"]
     W0 = synth.initial_w(k, R.m, seed=rank)
 
-    e = engine.Engine(R, k, lam, maxiter=max(args.steps, args.e2e_outer), maxinneriter=T, residual=args.residual,
-                      device=device, version=args.version, use_graph=bool(args.graph), relabel=bool(args.relabel))
-    e.set_factors(W0)
-    e.run(args.warmup)
-    # timed: device-resident
-    dist.barrier()
-    with ClockSampler(device) as clk:
-        rm = e.run(args.steps)
-        st = e.stats()
-    t_ms = dist.max(st["train_ms"])
-    dist.barrier()
-    updates = st["updates"]
-    value = ws * updates / (t_ms / 1e3)
-    launches = st["launches"]
-    # roofline pass: per-launch events around the sweeps
-    e.set_profiling(True)
-    e.run(2)
-    sp = e.stats()
-    e.set_profiling(False)
-    n_sweeps = sp["sweep_csc_launches"] + sp["sweep_csr_launches"]
-    sweep_ms = sp["sweep_csc_ms"] + sp["sweep_csr_ms"]
-    bytes_launch = sp["bytes_per_update"] / (2 * T)
-    mean_launch_s = sweep_ms / 1e3 / n_sweeps
+    def measure(residual):
+        """Device-resident timing of args.steps outer iterations + a roofline pass."""
+        e = engine.Engine(R, k, lam, maxiter=max(args.steps, args.e2e_outer), maxinneriter=T, residual=residual,
+                          device=device, version=args.version, use_graph=bool(args.graph),
+                          relabel=bool(args.relabel), layout=args.layout)
+        e.set_factors(W0)
+        e.run(args.warmup)
+        dist.barrier()
+        with ClockSampler(device) as clk:
+            rm = e.run(args.steps)
+            st = e.stats()
+        t_ms = dist.max(st["train_ms"])
+        dist.barrier()
+        # roofline pass: per-launch events around the sweeps
+        e.set_profiling(True)
+        e.run(2)
+        sp = e.stats()
+        e.set_profiling(False)
+        e.close()
+        n_sweeps = sp["sweep_csc_launches"] + sp["sweep_csr_launches"]
+        sweep_ms = sp["sweep_csc_ms"] + sp["sweep_csr_ms"]
+        bytes_launch = sp["bytes_per_update"] / (2 * T)
+        mean_launch_s = sweep_ms / 1e3 / n_sweeps
+        return dict(value=ws * st["updates"] / (t_ms / 1e3), t_ms=t_ms, launches=st["launches"],
+                    achieved=bytes_launch / mean_launch_s / 1e9, bytes_launch=bytes_launch,
+                    mean_launch_s=mean_launch_s, test_rmse=float(rm[-1]) if rm is not None else None,
+                    clocks=clk.summary(), refresh_ms_per_outer=sp["refresh_ms"] / 2, rmse_ms_per_outer=sp["rmse_ms"] / 2)
+
+    head = measure(args.residual)
+    comp = measure(args.compare) if args.compare != "none" else None
+    value, t_ms, launches = head["value"], head["t_ms"], head["launches"]
+    achieved, bytes_launch, mean_launch_s = head["achieved"], head["bytes_launch"], head["mean_launch_s"]
+    test_rmse = head["test_rmse"]
     peak, peak_kind = measured_peak()
-    achieved = bytes_launch / mean_launch_s / 1e9
     tr = profiled_traffic()
     traffic = None
     if tr and tr.get("workload") == WORKLOAD and tr.get("residual") == args.residual:
         traffic = tr.get("dram_bytes_per_launch")
-    test_rmse = float(rm[-1]) if rm is not None else None
-    e.close()
 
     if args.quick:
         args.no_cpu = True
@@ -272,7 +284,7 @@ def main():
     dist.close()
     if rank != 0:
         return
-    clocks = clk.summary()
+    clocks = head["clocks"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -281,7 +293,7 @@ def main():
         "config": {"workload": f"{WORKLOAD} {R.m}x{R.n} train_nnz={R.nnz} test_nnz={R.nnz_test} k={k} "
                                f"lambda={lam} T={T}",
                    "residual": args.residual, "version": args.version, "cuda_graph": bool(args.graph),
-                   "relabel": bool(args.relabel),
+                   "relabel": bool(args.relabel), "layout": args.layout,
                    "step": "one outer iteration (k rank-one updates + test RMSE)",
                    "l2": "no flush: the residual copies streamed every feature exceed L2",
                    "parallelism": f"replicas x{ws}"},
@@ -292,11 +304,20 @@ def main():
         "clocks": clocks,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": ("tile_sweep_kernel" if args.version == 3 else "sweep_kernel") + " (CSC h-sweep + CSR w-sweep)",
+                     "kernel": ("blocked_sweep_kernel + blocked_combine_kernel" if args.layout == "blocked" else
+                                "tile_sweep_kernel" if args.version == 3 else "sweep_kernel")
+                               + " (CSC h-sweep + CSR w-sweep)",
                      "bytes_per_launch": bytes_launch, "mean_launch_ms": mean_launch_s * 1e3},
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
+    if comp is not None:
+        line["comparison"] = {"residual": args.compare, "value": comp["value"], "unit": UNIT,
+                              "ms_per_step": comp["t_ms"] / args.steps, "test_rmse": comp["test_rmse"],
+                              "roofline_frac": comp["achieved"] / peak, "hbm_gbs_sweeps": comp["achieved"]}
+        line["mixed_vs_fp32"] = value / comp["value"] if args.compare == "f32" else None
+    line["refresh_ms_per_outer"] = head["refresh_ms_per_outer"]
+    line["rmse_ms_per_outer"] = head["rmse_ms_per_outer"]
     print(json.dumps(line), flush=True)
 
 
@@ -360,7 +381,7 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
     d2h = W0.nbytes + 4 * k * R.n + 8 * args.e2e_outer
     Wp[...] = W0
     kw = dict(residual=args.residual, device=device, version=args.version, use_graph=bool(args.graph),
-              relabel=bool(args.relabel))
+              relabel=bool(args.relabel), layout=args.layout)
     engine.train(Rp, Wp, k, lam, 1, T, **kw)  # warm the context
     dist.barrier()
     t0 = time.perf_counter()

@@ -24,7 +24,7 @@ NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I",
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-I", INC]
 
 CU_SOURCES = ["engine.cu"]
-CXX_SOURCES = ["synth.cpp", "relabel.cpp"]
+CXX_SOURCES = ["synth.cpp", "relabel.cpp", "blocked.cpp"]
 CLI_SOURCES = ["cli/main.cpp", "cli/loader.cpp"]
 
 

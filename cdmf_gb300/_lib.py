@@ -39,7 +39,7 @@ class Opts(ctypes.Structure):
         ("maxinneriter", ctypes.c_int32), ("version", ctypes.c_int32), ("residual", ctypes.c_int32),
         ("reduce", ctypes.c_int32), ("rmse_each_outer", ctypes.c_int32), ("use_graph", ctypes.c_int32),
         ("threads_per_block", ctypes.c_int32), ("device", ctypes.c_int32), ("verbose", ctypes.c_int32),
-        ("relabel", ctypes.c_int32), ("autotune", ctypes.c_int32),
+        ("relabel", ctypes.c_int32), ("autotune", ctypes.c_int32), ("layout", ctypes.c_int32),
     ]
 
 

@@ -21,7 +21,9 @@
 #include "sweep_kernels.cuh"
 #include "refresh_kernels.cuh"
 #include "tile_kernels.cuh"
+#include "blocked_kernels.cuh"
 #include "relabel.h"
+#include "blocked.h"
 
 #include <cuda_runtime.h>
 
@@ -55,6 +57,17 @@ struct DevTiles {
     uint32_t* lcount = nullptr;
     uint32_t* empty = nullptr;
     uint32_t ntiles = 0, nempty = 0, tile_blocks = 0, empty_blocks = 0;
+};
+
+// cross-index-blocked copy (layout 1)
+struct DevBlocked {
+    uint32_t* segptr = nullptr;
+    uint16_t* idx = nullptr;
+    uint32_t* units = nullptr;
+    float2* part = nullptr;
+    uint32_t* map = nullptr;     // line-layout position -> blocked position
+    uint32_t nunits = 0, nb = 0, lines = 0, xb = 0;
+    uint64_t cross = 0;
 };
 
 struct DevBins {
@@ -147,6 +160,10 @@ struct cdmf_handle {
     DevBins csr, csc;
     DevTiles tcsr, tcsc;
     bool tiles = false;              // version 3: nonzero-balanced tile sweeps
+    DevBlocked bcsr, bcsc;
+    bool blocked = false;            // layout 1: cross-index-blocked copies
+    std::vector<uint32_t> hmap_r, hmap_c;   // host copies of the blocked maps
+    uint32_t* ref_to_csr = nullptr;  // refresh: CSR line position -> CSR copy position (blocked)
     // degree relabelling: new id -> caller id, new position -> caller position
     bool relabeled = false;
     std::vector<uint32_t> row_old, col_old, csr_pos, csc_pos;
@@ -293,6 +310,26 @@ int upload_tiles(cdmf_handle* h, DevTiles& D, const uint32_t* ptr, int64_t lines
     return CDMF_OK;
 }
 
+int upload_blocked(cdmf_handle* h, DevBlocked& D, BlockedHost&& B, std::vector<uint32_t>& hmap) {
+    D.nb = B.nb;
+    D.lines = B.lines;
+    D.xb = B.xb;
+    D.cross = B.cross;
+    D.nunits = (uint32_t)(B.units.size() / 5);
+    int r;
+    if ((r = dalloc(h, &D.segptr, B.segptr.size())) || (r = dalloc(h, &D.idx, B.idx16.size())) ||
+        (r = dalloc(h, &D.units, B.units.size())) || (r = dalloc(h, &D.part, (size_t)B.nb * B.lines)) ||
+        (r = dalloc(h, &D.map, B.pos.size())))
+        return r;
+    CU(h, cudaMemcpyAsync(D.segptr, B.segptr.data(), 4 * B.segptr.size(), cudaMemcpyHostToDevice, h->s));
+    if (!B.idx16.empty()) CU(h, cudaMemcpyAsync(D.idx, B.idx16.data(), 2 * B.idx16.size(), cudaMemcpyHostToDevice, h->s));
+    CU(h, cudaMemcpyAsync(D.units, B.units.data(), 4 * B.units.size(), cudaMemcpyHostToDevice, h->s));
+    if (!B.pos.empty()) CU(h, cudaMemcpyAsync(D.map, B.pos.data(), 4 * B.pos.size(), cudaMemcpyHostToDevice, h->s));
+    CU(h, cudaStreamSynchronize(h->s));
+    hmap = std::move(B.pos);
+    return CDMF_OK;
+}
+
 cudaEvent_t pool_event(cdmf_handle* h) {
     if (h->pool_used == h->pool.size()) {
         cudaEvent_t e;
@@ -400,7 +437,67 @@ SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const
     return A;
 }
 
+template <int RT, int MODE, bool SUB, bool ADD>
+void blocked_launch(const BlockedArgs& B, unsigned grid, cudaStream_t s) {
+    using T = typename Tbl<MODE>::T;
+    blocked_sweep_kernel<RT, MODE, SUB, ADD><<<grid, kBlock, B.xb * sizeof(T), s>>>(B);
+}
+
+template <int RT, int MODE>
+void blocked_mode(const BlockedArgs& B, bool sub, bool add, unsigned grid, cudaStream_t s) {
+    if (MODE == M_PLAIN) blocked_launch<RT, M_PLAIN, false, false>(B, grid, s);
+    else if (sub && add) blocked_launch<RT, MODE, true, true>(B, grid, s);
+    else if (sub) blocked_launch<RT, MODE, true, false>(B, grid, s);
+    else if (add) blocked_launch<RT, MODE, false, true>(B, grid, s);
+    else blocked_launch<RT, MODE, false, false>(B, grid, s);
+}
+
+template <int RT>
+void blocked_rt(const BlockedArgs& B, int mode, bool sub, bool add, unsigned grid, cudaStream_t s) {
+    if (mode == M_CSC) blocked_mode<RT, M_CSC>(B, sub, add, grid, s);
+    else if (mode == M_CSR) blocked_mode<RT, M_CSR>(B, sub, add, grid, s);
+    else blocked_mode<RT, M_PLAIN>(B, false, false, grid, s);
+}
+
+int launch_blocked(cdmf_handle* h, int kind, const SweepArgs& A, int mode, bool sub, bool add) {
+    const DevBlocked& D = kind == K_CSC ? h->bcsc : h->bcsr;
+    BlockedArgs B;
+    B.segptr = D.segptr;
+    B.idx = D.idx;
+    B.res = A.res;
+    B.table = mode == M_CSC ? (const void*)A.P : mode == M_CSR ? (const void*)A.Q : (const void*)A.y;
+    B.b = A.b;
+    B.d = A.d;
+    B.part = D.part;
+    B.units = D.units;
+    B.xb = D.xb;
+    B.lines = D.lines;
+    B.cross = D.cross;
+    {
+        Timed tm(h, kind);
+        if (D.nunits) {
+            switch (h->rt) {
+                case 0: blocked_rt<0>(B, mode, sub, add, D.nunits, h->s); break;
+                case 1: blocked_rt<1>(B, mode, sub, add, D.nunits, h->s); break;
+                default: blocked_rt<2>(B, mode, sub, add, D.nunits, h->s); break;
+            }
+        }
+        const unsigned cg = (D.lines + kBlock - 1) / kBlock;
+        if (cg) {
+            if (mode == M_CSC) blocked_combine_kernel<M_CSC><<<cg, kBlock, 0, h->s>>>(A, D.segptr, D.part, D.nb, D.lines);
+            else if (mode == M_CSR) blocked_combine_kernel<M_CSR><<<cg, kBlock, 0, h->s>>>(A, D.segptr, D.part, D.nb, D.lines);
+            else blocked_combine_kernel<M_PLAIN><<<cg, kBlock, 0, h->s>>>(A, D.segptr, D.part, D.nb, D.lines);
+        }
+    }
+    CU(h, cudaGetLastError());
+    h->st.launches += 2;
+    if (kind == K_CSC) h->st.sweep_csc_launches++;
+    else h->st.sweep_csr_launches++;
+    return CDMF_OK;
+}
+
 int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A, int mode, bool sub, bool add) {
+    if (h->blocked) return launch_blocked(h, kind, A, mode, sub, add);
     if (h->tiles) {
         const DevTiles& D3 = kind == K_CSC ? h->tcsc : h->tcsr;
         TileArgs T;
@@ -538,6 +635,28 @@ int flush_pending(cdmf_handle* h) {
     const int tp = h->pending;
     const float* Wp = h->W + (size_t)tp * h->m;
     const float* Hp = h->H + (size_t)tp * h->n;
+    if (h->blocked) {
+        const DevBlocked& C = h->bcsc;
+        const DevBlocked& R = h->bcsr;
+        switch (h->rt) {
+            case 0:
+                blocked_flush_kernel<0><<<2048, kBlock, 0, h->s>>>(C.segptr, C.idx, h->res_csc, Wp, Hp, C.nb, C.lines, C.xb);
+                blocked_flush_kernel<0><<<2048, kBlock, 0, h->s>>>(R.segptr, R.idx, h->res_csr, Hp, Wp, R.nb, R.lines, R.xb);
+                break;
+            case 1:
+                blocked_flush_kernel<1><<<2048, kBlock, 0, h->s>>>(C.segptr, C.idx, h->res_csc, Wp, Hp, C.nb, C.lines, C.xb);
+                blocked_flush_kernel<1><<<2048, kBlock, 0, h->s>>>(R.segptr, R.idx, h->res_csr, Hp, Wp, R.nb, R.lines, R.xb);
+                break;
+            default:
+                blocked_flush_kernel<2><<<2048, kBlock, 0, h->s>>>(C.segptr, C.idx, h->res_csc, Wp, Hp, C.nb, C.lines, C.xb);
+                blocked_flush_kernel<2><<<2048, kBlock, 0, h->s>>>(R.segptr, R.idx, h->res_csr, Hp, Wp, R.nb, R.lines, R.xb);
+                break;
+        }
+        CU(h, cudaGetLastError());
+        h->pending = -1;
+        h->p_for = -1;
+        return CDMF_OK;
+    }
     const unsigned gc = (unsigned)std::min<int64_t>(4096, (h->n + kWarps - 1) / kWarps + 1);
     const unsigned gr = (unsigned)std::min<int64_t>(4096, (h->m + kWarps - 1) / kWarps + 1);
     switch (h->rt) {
@@ -572,12 +691,12 @@ int refresh_residual(cdmf_handle* h) {
         if (h->m) to_row_major_kernel<<<gw, kBlock, 0, h->s>>>(h->W, h->Wrm, h->o.k, h->kp, h->m);
         if (h->n) to_row_major_kernel<<<gh, kBlock, 0, h->s>>>(h->H, h->Hrm, h->o.k, h->kp, h->n);
         if (h->rt == 1)
-            refresh_kernel<1><<<h->ref_grid, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->csr_val, h->to_csc, h->m,
+            refresh_kernel<1><<<h->ref_grid, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->csr_val, h->ref_to_csr, h->to_csc, h->m,
                                                                h->nnz, h->Wrm, h->Hrm, h->kp, h->res_csr, h->res_csc,
                                                                pa, pb, h->ref_part, h->ref_count, h->drift_out,
                                                                h->nonfinite);
         else
-            refresh_kernel<2><<<h->ref_grid, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->csr_val, h->to_csc, h->m,
+            refresh_kernel<2><<<h->ref_grid, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->csr_val, h->ref_to_csr, h->to_csc, h->m,
                                                                h->nnz, h->Wrm, h->Hrm, h->kp, h->res_csr, h->res_csc,
                                                                pa, pb, h->ref_part, h->ref_count, h->drift_out,
                                                                h->nonfinite);
@@ -606,6 +725,14 @@ __global__ void res_to_f32_kernel(const void* __restrict__ src, float* __restric
 // dst residual := src ratings (device, float)
 int reset_residual(cdmf_handle* h, void* dst, const float* src) {
     if (h->nnz == 0) return CDMF_OK;
+    if (h->blocked) {
+        const uint32_t* map = dst == h->res_csr ? h->bcsr.map : h->bcsc.map;
+        if (h->rt == 0) scatter_res_kernel<0><<<1216, 256, 0, h->s>>>(src, map, dst, h->nnz);
+        else if (h->rt == 1) scatter_res_kernel<1><<<1216, 256, 0, h->s>>>(src, map, dst, h->nnz);
+        else scatter_res_kernel<2><<<1216, 256, 0, h->s>>>(src, map, dst, h->nnz);
+        CU(h, cudaGetLastError());
+        return CDMF_OK;
+    }
     if (h->rt == 0) {
         CU(h, cudaMemcpyAsync(dst, src, sizeof(float) * h->nnz, cudaMemcpyDeviceToDevice, h->s));
     } else {
@@ -762,6 +889,9 @@ void cdmf_opts_default(cdmf_opts* o) {
     o->threads_per_block = 0;
     o->device = 0;
     o->verbose = 0;
+    o->relabel = 1;
+    o->autotune = 0;
+    o->layout = CDMF_LAYOUT_LINES;
 }
 
 const char* cdmf_cuda_strerror(int status) {
@@ -885,6 +1015,17 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         (r = up(h->te_val, p->test_val, 4 * h->nt)))
         return bail(r);
     if (cudaMemsetAsync(h->rmse_count, 0, 4, h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    const bool seq = o->reduce == CDMF_REDUCE_SEQUENTIAL;
+    h->blocked = o->layout == 1 && !seq && N > 0;
+    if (h->blocked) {
+        BlockedHost br, bc;
+        if (!build_blocked(p->csr_row_ptr, p->csr_col_idx, (uint32_t)m, (uint64_t)n, kXbCol, kUnitNnz, br) ||
+            !build_blocked(p->csc_col_ptr, p->csc_row_idx, (uint32_t)n, (uint64_t)m, kXbRow, kUnitNnz, bc))
+            return bail(CDMF_ERR_ALLOC);
+        if ((r = upload_blocked(h, h->bcsr, std::move(br), h->hmap_r)) ||
+            (r = upload_blocked(h, h->bcsc, std::move(bc), h->hmap_c)))
+            return bail(r);
+    }
     if (h->rt != 0) {
         // CSR position -> CSC position; also proves the CSC arrays are the
         // transpose of the CSR arrays, which the refresh scatter relies on
@@ -905,6 +1046,11 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
             (r = dalloc(h, &h->Hrm, (size_t)n * h->kp)) || (r = dalloc(h, &h->ref_part, h->ref_grid)) ||
             (r = dalloc(h, &h->drift_out, 1)) || (r = dalloc(h, &h->ref_count, 1)) || (r = dalloc(h, &h->nonfinite, 1)))
             return bail(r);
+        if (h->blocked) {
+            // the refresh writes both copies at their blocked positions
+            for (int64_t q = 0; q < N; ++q) to_csc[q] = h->hmap_c[to_csc[q]];
+            h->ref_to_csr = h->bcsr.map;
+        }
         if ((r = up(h->to_csc, to_csc.data(), 4 * N))) return bail(r);
         if (cudaMemsetAsync(h->ref_count, 0, 4, h->s) != cudaSuccess ||
             cudaMemsetAsync(h->nonfinite, 0, 8, h->s) != cudaSuccess ||
@@ -912,14 +1058,13 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
             cudaStreamSynchronize(h->s) != cudaSuccess)
             return bail(CDMF_ERR_CUDA);
     }
-    const bool seq = o->reduce == CDMF_REDUCE_SEQUENTIAL;
     h->seq = seq;
     h->hptr_r.assign(p->csr_row_ptr, p->csr_row_ptr + m + 1);
     h->hptr_c.assign(p->csc_col_ptr, p->csc_col_ptr + n + 1);
     if ((r = upload_bins(h, h->csr, plan_bins(p->csr_row_ptr, m, seq, h->cfg))) ||
         (r = upload_bins(h, h->csc, plan_bins(p->csc_col_ptr, n, seq, h->cfg))))
         return bail(r);
-    h->tiles = o->version == 3 && !seq;
+    h->tiles = o->version == 3 && !seq && !h->blocked;
     if (h->tiles && ((r = upload_tiles(h, h->tcsr, p->csr_row_ptr, m, N)) ||
                      (r = upload_tiles(h, h->tcsc, p->csc_col_ptr, n, N))))
         return bail(r);
@@ -933,7 +1078,8 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if (o->autotune && (r = cdmf_cuda_autotune(h, nullptr, nullptr))) return bail(r);
     const double T = std::max(1, o->maxinneriter);
     const double br = (double)h->rbytes;
-    h->st.bytes_per_update = T * 2.0 * N * (4.0 + br) + 2.0 * N * br + T * 4.0 * (m + n + 2) + 8.0 * (m + n);
+    const double bi = h->blocked ? 2.0 : 4.0;   // index bytes as stored
+    h->st.bytes_per_update = T * 2.0 * N * (bi + br) + 2.0 * N * br + T * 4.0 * (m + n + 2) + 8.0 * (m + n);
     *out = h;
     return CDMF_OK;
 }
@@ -1075,13 +1221,21 @@ int cdmf_cuda_get_state(cdmf_handle* h, float* W, float* H, float* res_csc, floa
         }
         return CDMF_OK;
     };
-    std::vector<float> tc, tr;
+    std::vector<float> tc, tr, bc, bq;
     float* dc = res_csc;
     float* dr = res_csr;
     if (h->relabeled && res_csc) { tc.resize(h->nnz); dc = tc.data(); }
     if (h->relabeled && res_csr) { tr.resize(h->nnz); dr = tr.data(); }
-    if ((r = down(dc, h->res_csc)) || (r = down(dr, h->res_csr))) return r;
+    float* gc = dc;
+    float* gr = dr;
+    if (h->blocked && dc) { bc.resize(h->nnz); gc = bc.data(); }
+    if (h->blocked && dr) { bq.resize(h->nnz); gr = bq.data(); }
+    if ((r = down(gc, h->res_csc)) || (r = down(gr, h->res_csr))) return r;
     CU(h, cudaStreamSynchronize(h->s));
+    if (h->blocked) {   // blocked positions -> line-layout positions
+        if (dc) for (int64_t o = 0; o < h->nnz; ++o) dc[o] = gc[h->hmap_c[o]];
+        if (dr) for (int64_t o = 0; o < h->nnz; ++o) dr[o] = gr[h->hmap_r[o]];
+    }
     if (h->relabeled) {
         if (res_csc) for (int64_t o = 0; o < h->nnz; ++o) res_csc[h->csc_pos[o]] = dc[o];
         if (res_csr) for (int64_t o = 0; o < h->nnz; ++o) res_csr[h->csr_pos[o]] = dr[o];
@@ -1111,6 +1265,17 @@ int cdmf_cuda_set_state(cdmf_handle* h, const float* W, const float* H, const fl
         }
         res_csc = tc.data();
         res_csr = tr.data();
+    }
+    std::vector<float> bc, bq;
+    if (h->blocked && h->nnz > 0) {   // line-layout positions -> blocked positions
+        bc.resize(h->nnz);
+        bq.resize(h->nnz);
+        for (int64_t o = 0; o < h->nnz; ++o) {
+            bc[h->hmap_c[o]] = res_csc[o];
+            bq[h->hmap_r[o]] = res_csr[o];
+        }
+        res_csc = bc.data();
+        res_csr = bq.data();
     }
     CU(h, cudaMemcpyAsync(h->W, W, sizeof(float) * h->o.k * h->m, cudaMemcpyHostToDevice, h->s));
     CU(h, cudaMemcpyAsync(h->H, H, sizeof(float) * h->o.k * h->n, cudaMemcpyHostToDevice, h->s));
@@ -1577,6 +1742,7 @@ int cdmf_cuda_batch_create(const cdmf_problem* probs, const cdmf_opts* opts, int
         cdmf_opts o = opts[q];
         o.version = 1;        // grouped sweeps use the binned kernel
         o.use_graph = 0;
+        o.layout = CDMF_LAYOUT_LINES;
         cdmf_handle* h = nullptr;
         const int r = cdmf_cuda_create(probs + q, &o, &h);
         if (r) return bail(r);

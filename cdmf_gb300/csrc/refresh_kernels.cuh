@@ -5,8 +5,9 @@
 // incremental update rounds, so once per outer iteration the residual is
 // recomputed from the FP32 ratings and the FP32 factors:
 //     r_ij = R_ij - sum_t W[t][i] * H[t][j]
-// in CSR order (coalesced over the ratings), written to the CSR copy in place
-// and scattered to the CSC copy through the CSR->CSC position map.  The
+// in CSR order (coalesced over the ratings), written to the CSR copy (in
+// place, or through a position map when the copies are blocked) and
+// scattered to the CSC copy through the CSR->CSC position map.  The
 // scatter is L2-friendly: rows are visited in increasing order, so the
 // writes into a column's segment advance monotonically and partial sectors
 // merge in L2.  The same pass measures, in FP64, how far the stored residual
@@ -45,7 +46,7 @@ __global__ void __launch_bounds__(kBlock) to_row_major_kernel(const float* __res
 template <int RT>
 __global__ void __launch_bounds__(kBlock) refresh_kernel(
     const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ idx, const float* __restrict__ val,
-    const uint32_t* __restrict__ to_csc, int64_t m, int64_t nnz, const float* __restrict__ Wrm,
+    const uint32_t* __restrict__ to_csr, const uint32_t* __restrict__ to_csc, int64_t m, int64_t nnz, const float* __restrict__ Wrm,
     const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr, void* __restrict__ res_csc,
     const float* __restrict__ pa, const float* __restrict__ pb_,  // pending subtract: a = H[tp] (cols), b = W[tp] (rows)
     double* part, uint32_t* counter, double* drift_out, unsigned long long* nonfinite_out) {
@@ -97,9 +98,10 @@ __global__ void __launch_bounds__(kBlock) refresh_kernel(
                 dot = fmaf(w.w, h.w, dot);
             }
             const float rnew = __fsub_rn(__ldg(val + p), dot);
-            float rold = Res<RT>::ld(res_csr, (uint32_t)p);
+            const uint32_t pr = to_csr ? __ldg(to_csr + p) : (uint32_t)p;
+            float rold = Res<RT>::ld(res_csr, pr);
             if (pa) rold = __fsub_rn(rold, __fmul_rn(__ldg(pa + j), __ldg(pb_ + i)));
-            const float stored = Res<RT>::st(res_csr, (uint32_t)p, rnew);
+            const float stored = Res<RT>::st(res_csr, pr, rnew);
             Res<RT>::st(res_csc, __ldg(to_csc + p), rnew);
             if (!isfinite(stored)) bad++;
             const double d = (double)rnew - (double)rold;

@@ -47,7 +47,7 @@ def _problem(R):
 
 def make_opts(k, lambda_, maxiter=5, maxinneriter=5, version=1, residual="f32", reduce="tree",
               rmse_each_outer=True, use_graph=False, device=0, threads_per_block=0, verbose=0, relabel=True,
-              autotune=False):
+              autotune=False, layout=None):
     o = _lib.Opts()
     _lib.load().cdmf_opts_default(ctypes.byref(o))
     o.k, o.lambda_, o.maxiter, o.maxinneriter = int(k), float(lambda_), int(maxiter), int(maxinneriter)
@@ -59,6 +59,8 @@ def make_opts(k, lambda_, maxiter=5, maxinneriter=5, version=1, residual="f32", 
     o.device, o.threads_per_block, o.verbose = int(device), int(threads_per_block), int(verbose)
     o.relabel = int(bool(relabel))
     o.autotune = int(bool(autotune))
+    if layout is not None:
+        o.layout = {"lines": 0, "blocked": 1}[layout] if isinstance(layout, str) else int(layout)
     return o
 
 

@@ -91,7 +91,13 @@ typedef struct {
                                  (tree order only; results come back in the caller's numbering) */
     int32_t autotune;         /* 1: pick the bin thresholds by timing candidates on this matrix
                                  at create (cached per matrix shape in the process) */
+    int32_t layout;           /* CDMF_LAYOUT_*: how the residual copies are stored (tree order) */
 } cdmf_opts;
+
+/* Residual copy layout (cdmf_opts.layout). */
+#define CDMF_LAYOUT_LINES 0    /* CSR / CSC as given; row-length-binned sweeps */
+#define CDMF_LAYOUT_BLOCKED 1  /* cross-index blocks: gather tables staged in shared memory,
+                                  16-bit indices; used with tree order only */
 
 /* Line-length bin thresholds of the binned sweeps (versions 1/2), in
  * nonzeros: <= thread_max one thread per line, <= group_max 8 lanes,

@@ -344,3 +344,83 @@ def test_autotune_and_bincfg(cpu_scale):
     with pytest.raises(Exception):
         with engine.Engine(R, run["k"], run["lambda_"], 1, 1) as e:
             e.set_bincfg(warp_max=100, cta_max=50)
+
+
+# ---- cross-index-blocked layout ---------------------------------------------
+
+@pytest.mark.parametrize("name", ["mini", "simple", "tricky_simple"])
+def test_blocked_within_fp32_budget_each_outer(name):
+    R, z = load_golden(name)
+    md = META[name]
+    r64 = oracle.ccdpp(R, z["W0"].astype(np.float64), md["k"], md["lam"], md["maxiter"], md["maxinner"],
+                       dtype=np.float64, history=True)
+    with engine.Engine(R, md["k"], md["lam"], md["maxiter"], md["maxinner"], layout="blocked") as e:
+        e.set_factors(z["W0"])
+        for j in range(md["maxiter"]):
+            rm = e.run(1)
+            W, H = e.factors()
+            okw, gw = within_budget(W, z["W_hist"][j], r64["W_hist"][j])
+            okh, gh = within_budget(H, z["H_hist"][j], r64["H_hist"][j])
+            assert okw and okh, (j, gw, gh)
+            assert rmse_ok(rm[0], z["rmse"][j], r64["rmse"][j])
+
+
+def test_blocked_cpu_scale_one_step_and_free(cpu_scale):
+    R, run, W0, ref = cpu_scale
+    k, lam, T = run["k"], run["lambda_"], run["maxinneriter"]
+    with engine.Engine(R, k, lam, run["maxiter"], T, layout="blocked") as e:
+        e.set_factors(W0)
+        rm = e.run(run["maxiter"])
+        W, H = e.factors()
+        okw, gw = within_budget(W, ref["W"], ref["f64"]["W"])
+        okh, gh = within_budget(H, ref["H"], ref["f64"]["H"])
+        assert okw and okh, (gw, gh)
+        assert all(rmse_ok(a, b, c) for a, b, c in zip(rm, ref["rmse"], ref["f64"]["rmse"]))
+        # one step from the oracle's state after outer 2
+        Wst, Hst = ref["W_hist"][1].copy(), ref["H_hist"][1].copy()
+        r2 = oracle.ccdpp(R, W0, k, lam, 2, T, threads=8, residuals=True)
+        e.set_state(Wst, Hst, r2["res_csc"], r2["res_csr"], 3)
+        rm = e.run(1)
+        Wg, Hg = e.factors()
+        W64, H64 = Wst.astype(np.float64), Hst.astype(np.float64)
+        rc64, rr64 = r2["res_csc"].astype(np.float64), r2["res_csr"].astype(np.float64)
+        oracle.outer_iteration(R, W64, H64, rc64, rr64, k, lam, T, 3, threads=8)
+        okw, gw = within_budget(Wg, ref["W_hist"][2], W64)
+        okh, gh = within_budget(Hg, ref["H_hist"][2], H64)
+        assert okw and okh, (gw, gh)
+
+
+@pytest.mark.parametrize("residual", ["bf16", "f16"])
+def test_blocked_mixed_residual(cpu_scale, residual):
+    R, run, W0, ref = cpu_scale
+    r64 = ref["f64"]
+    with engine.Engine(R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"], residual=residual,
+                       layout="blocked", use_graph=True) as e:
+        e.set_factors(W0)
+        rm = e.run(run["maxiter"])
+        st = e.stats()
+        state = e.state()
+    assert np.max(np.abs(rm - r64["rmse"])) <= 1e-3, (rm, r64["rmse"])
+    assert st["nonfinite"] == 0 and 0.0 < st["drift_rms"] < 5e-2
+    rows, cols, vals = R.coo()
+    exact = vals.astype(np.float64) - np.einsum("ti,ti->i", state["W"][:, rows].astype(np.float64),
+                                                state["H"][:, cols].astype(np.float64))
+    assert np.sqrt(np.mean((state["res_csr"] - exact) ** 2)) < 5e-2
+
+
+def test_blocked_deterministic_and_state_roundtrip(cpu_scale):
+    R, run, W0, ref = cpu_scale
+    outs = []
+    for split in (False, True):
+        with engine.Engine(R, run["k"], run["lambda_"], 4, 1, layout="blocked") as e:
+            e.set_factors(W0)
+            if split:
+                e.run(2)
+                st = e.state()
+                e.set_state(st["W"], st["H"], st["res_csc"], st["res_csr"], st["next_oiter"])
+                e.run(2)
+            else:
+                e.run(4)
+            outs.append(e.state())
+    for f in ("W", "H", "res_csc", "res_csr"):
+        assert np.array_equal(bits(outs[0][f]), bits(outs[1][f])), f
