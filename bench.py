@@ -233,9 +233,11 @@ def main():
 
     def measure(residual):
         """Device-resident timing of args.steps outer iterations + a roofline pass."""
+        t_create = time.perf_counter()
         e = engine.Engine(R, k, lam, maxiter=max(args.steps, args.e2e_outer), maxinneriter=T, residual=residual,
                           device=device, version=args.version, use_graph=bool(args.graph),
                           relabel=bool(args.relabel), layout=args.layout)
+        t_create = time.perf_counter() - t_create
         e.set_factors(W0)
         e.run(args.warmup)
         dist.barrier()
@@ -257,7 +259,8 @@ def main():
         return dict(value=ws * st["updates"] / (t_ms / 1e3), t_ms=t_ms, launches=st["launches"],
                     achieved=bytes_launch / mean_launch_s / 1e9, bytes_launch=bytes_launch,
                     mean_launch_s=mean_launch_s, test_rmse=float(rm[-1]) if rm is not None else None,
-                    clocks=clk.summary(), refresh_ms_per_outer=sp["refresh_ms"] / 2, rmse_ms_per_outer=sp["rmse_ms"] / 2)
+                    clocks=clk.summary(), refresh_ms_per_outer=sp["refresh_ms"] / 2, rmse_ms_per_outer=sp["rmse_ms"] / 2,
+                    create_s=t_create)
 
     head = measure(args.residual)
     comp = measure(args.compare) if args.compare != "none" else None
@@ -317,6 +320,7 @@ def main():
                               "roofline_frac": comp["achieved"] / peak, "hbm_gbs_sweeps": comp["achieved"]}
         line["mixed_vs_fp32"] = value / comp["value"] if args.compare == "f32" else None
     line["refresh_ms_per_outer"] = head["refresh_ms_per_outer"]
+    line["create_s"] = head["create_s"]
     line["rmse_ms_per_outer"] = head["rmse_ms_per_outer"]
     print(json.dumps(line), flush=True)
 
