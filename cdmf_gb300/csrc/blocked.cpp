@@ -1,7 +1,10 @@
-// Cross-index-blocked layout builder (see blocked.h).
+// Cross-index-blocked layout builder (see blocked.h).  The counting and the
+// fill run in parallel over lines: segment (b, j) belongs to line j alone,
+// so threads never share a counter.
 #include "blocked.h"
 
 #include <algorithm>
+#include <omp.h>
 
 namespace cdmf {
 
@@ -19,19 +22,25 @@ bool build_blocked(const uint32_t* ptr, const uint32_t* idx, uint32_t lines, uin
         B.segptr.assign(nseg + 1, 0);
         // count per segment: a line's entries are sorted, so its segments are
         // consecutive runs of its range
-        for (uint32_t j = 0; j < lines; ++j)
+#pragma omp parallel for schedule(dynamic, 1024)
+        for (int64_t j = 0; j < (int64_t)lines; ++j)
             for (uint32_t p = ptr[j]; p < ptr[j + 1]; ++p) B.segptr[(uint64_t)(idx[p] / xb) * lines + j + 1]++;
         for (uint64_t s = 0; s < nseg; ++s) B.segptr[s + 1] += B.segptr[s];
+        if (B.segptr[nseg] != nnz) return false;
         B.idx16.resize(nnz);
         B.pos.resize(nnz);
-        std::vector<uint32_t> next(B.segptr.begin(), B.segptr.end() - 1);
-        for (uint32_t j = 0; j < lines; ++j)
-            for (uint32_t p = ptr[j]; p < ptr[j + 1]; ++p) {
+#pragma omp parallel for schedule(dynamic, 1024)
+        for (int64_t j = 0; j < (int64_t)lines; ++j) {
+            uint32_t p = ptr[j];
+            while (p < ptr[j + 1]) {
                 const uint32_t b = idx[p] / xb;
-                const uint32_t q = next[(uint64_t)b * lines + j]++;
-                B.idx16[q] = (uint16_t)(idx[p] - b * xb);
-                B.pos[p] = q;
+                uint32_t q = B.segptr[(uint64_t)b * lines + j];
+                for (; p < ptr[j + 1] && idx[p] / xb == b; ++p, ++q) {
+                    B.idx16[q] = (uint16_t)(idx[p] - b * xb);
+                    B.pos[p] = q;
+                }
             }
+        }
         // work units: consecutive lines of one block up to ~unit_nnz nonzeros,
         // with the line ranges handled by the whole CTA (segments >= cta_len),
         // by single warps (>= warp_len) and by 8-lane groups (the rest);

@@ -12,6 +12,8 @@
 // shared-memory read; each segment leaves a partial sum, and a second
 // kernel adds a line's partials in block order.
 #pragma once
+#include "relabel.h"
+
 #include <cstdint>
 #include <vector>
 
@@ -21,8 +23,8 @@ struct BlockedHost {
     uint32_t xb = 0, nb = 0, lines = 0;
     uint64_t cross = 0;
     std::vector<uint32_t> segptr;       // nb * lines + 1
-    std::vector<uint16_t> idx16;        // nnz: cross index - b * xb
-    std::vector<uint32_t> pos;          // position in the line layout -> blocked position
+    uvec<uint16_t> idx16;               // nnz: cross index - b * xb
+    uvec<uint32_t> pos;                 // position in the line layout -> blocked position
     std::vector<uint32_t> units;        // 5 per unit: b, first line, end of CTA lines, end of warp lines, end line
 };
 

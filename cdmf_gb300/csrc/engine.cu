@@ -162,11 +162,12 @@ struct cdmf_handle {
     bool tiles = false;              // version 3: nonzero-balanced tile sweeps
     DevBlocked bcsr, bcsc;
     bool blocked = false;            // layout 1: cross-index-blocked copies
-    std::vector<uint32_t> hmap_r, hmap_c;   // host copies of the blocked maps
+    uvec<uint32_t> hmap_r, hmap_c;   // host copies of the blocked maps
     uint32_t* ref_to_csr = nullptr;  // refresh: CSR line position -> CSR copy position (blocked)
     // degree relabelling: new id -> caller id, new position -> caller position
     bool relabeled = false;
-    std::vector<uint32_t> row_old, col_old, csr_pos, csc_pos;
+    uvec<uint32_t> row_old, col_old, csr_pos, csc_pos, csc_from_csr;
+    uvec<uint32_t> ucsr_ptr, ucsr_idx;   // caller's CSR structure, for csc_pos on demand
     // host copies of the line pointers (engine numbering) and the bin plan
     std::vector<uint32_t> hptr_r, hptr_c;
     BinCfg cfg;
@@ -234,11 +235,13 @@ int dalloc(cdmf_handle* h, T** p, size_t count) {
 int check_compressed(const uint32_t* ptr, const uint32_t* idx, int64_t lines, int64_t cross, int64_t nnz) {
     if (!ptr || (nnz > 0 && !idx)) return CDMF_ERR_INVALID;
     if (ptr[0] != 0 || (int64_t)ptr[lines] != nnz) return CDMF_ERR_INVALID;
-    for (int64_t j = 0; j < lines; ++j)
-        if (ptr[j] > ptr[j + 1]) return CDMF_ERR_INVALID;
-    for (int64_t q = 0; q < nnz; ++q)
-        if ((int64_t)idx[q] >= cross) return CDMF_ERR_INVALID;
-    return CDMF_OK;
+    bool ok = true;
+#pragma omp parallel for schedule(static) reduction(&& : ok)
+    for (int64_t j = 0; j < lines; ++j) ok = ok && ptr[j] <= ptr[j + 1];
+    if (!ok) return CDMF_ERR_INVALID;
+#pragma omp parallel for schedule(static) reduction(&& : ok)
+    for (int64_t q = 0; q < nnz; ++q) ok = ok && (int64_t)idx[q] < cross;
+    return ok ? CDMF_OK : CDMF_ERR_INVALID;
 }
 
 int upload_bins(cdmf_handle* h, DevBins& D, Bins&& B) {
@@ -310,7 +313,7 @@ int upload_tiles(cdmf_handle* h, DevTiles& D, const uint32_t* ptr, int64_t lines
     return CDMF_OK;
 }
 
-int upload_blocked(cdmf_handle* h, DevBlocked& D, BlockedHost&& B, std::vector<uint32_t>& hmap) {
+int upload_blocked(cdmf_handle* h, DevBlocked& D, BlockedHost&& B, uvec<uint32_t>& hmap) {
     D.nb = B.nb;
     D.lines = B.lines;
     D.xb = B.xb;
@@ -437,9 +440,23 @@ SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const
     return A;
 }
 
+// Opts a kernel into `bytes` of dynamic shared memory (beyond the default
+// 48 KB including static) with the unified storage split toward shared memory.
+template <class K>
+void allow_smem(K kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::set<const void*> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.insert((const void*)kernel).second) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    }
+}
+
 template <int RT, int MODE, bool SUB, bool ADD>
 void blocked_launch(const BlockedArgs& B, unsigned grid, cudaStream_t s) {
     using T = typename Tbl<MODE>::T;
+    allow_smem(blocked_sweep_kernel<RT, MODE, SUB, ADD>, (size_t)kXbRow * sizeof(float4));
     blocked_sweep_kernel<RT, MODE, SUB, ADD><<<grid, kBlock, B.xb * sizeof(T), s>>>(B);
 }
 
@@ -744,19 +761,27 @@ int reset_residual(cdmf_handle* h, void* dst, const float* src) {
 
 // Caller numbering <-> engine numbering (identity unless relabelled).
 // X is k x len feature-major; `old_of_new` maps an engine id to a caller id.
-void gather_ids(const float* user, float* eng, uint32_t k, int64_t len, const std::vector<uint32_t>& old_of_new) {
+void gather_ids(const float* user, float* eng, uint32_t k, int64_t len, const uvec<uint32_t>& old_of_new) {
     for (uint32_t t = 0; t < k; ++t) {
         const float* u = user + (size_t)t * len;
         float* e = eng + (size_t)t * len;
         for (int64_t q = 0; q < len; ++q) e[q] = u[old_of_new[q]];
     }
 }
-void scatter_ids(const float* eng, float* user, uint32_t k, int64_t len, const std::vector<uint32_t>& old_of_new) {
+void scatter_ids(const float* eng, float* user, uint32_t k, int64_t len, const uvec<uint32_t>& old_of_new) {
     for (uint32_t t = 0; t < k; ++t) {
         const float* e = eng + (size_t)t * len;
         float* u = user + (size_t)t * len;
         for (int64_t q = 0; q < len; ++q) u[old_of_new[q]] = e[q];
     }
+}
+
+int need_csc_pos(cdmf_handle* h) {
+    if (!h->relabeled || !h->csc_pos.empty() || h->nnz == 0) return CDMF_OK;
+    if (!relabel_csc_positions(h->m, h->n, h->ucsr_ptr.data(), h->ucsr_idx.data(), h->csr_pos, h->csc_from_csr,
+                               h->csc_pos))
+        return fail(h, CDMF_ERR_ALLOC, "caller CSC positions");
+    return CDMF_OK;
 }
 
 // One outer iteration (src/cdmf_ref.cpp:69-137): refresh (16-bit modes),
@@ -956,6 +981,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
 
     const bool seq_order = o->reduce == CDMF_REDUCE_SEQUENTIAL;
     Relabel RL;
+    const cdmf_problem q0 = *p;
     cdmf_problem q = *p;
     if (o->relabel && !seq_order && p->nnz > 0) {
         if (!relabel(*p, RL)) return CDMF_ERR_INVALID;
@@ -975,7 +1001,9 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         h->row_old = std::move(RL.row_old);
         h->col_old = std::move(RL.col_old);
         h->csr_pos = std::move(RL.csr_pos);
-        h->csc_pos = std::move(RL.csc_pos);
+        h->csc_from_csr = std::move(RL.csc_from_csr);
+        h->ucsr_ptr.assign(q0.csr_row_ptr, q0.csr_row_ptr + q0.m + 1);
+        h->ucsr_idx.assign(q0.csr_col_idx, q0.csr_col_idx + q0.nnz);
     }
     h->o = *o;
     h->m = p->m;
@@ -1029,16 +1057,23 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if (h->rt != 0) {
         // CSR position -> CSC position; also proves the CSC arrays are the
         // transpose of the CSR arrays, which the refresh scatter relies on
-        std::vector<uint32_t> to_csc(N), next(p->csc_col_ptr, p->csc_col_ptr + n);
-        for (int64_t i = 0; i < m; ++i)
-            for (uint32_t q = p->csr_row_ptr[i]; q < p->csr_row_ptr[i + 1]; ++q) {
-                const uint32_t j = p->csr_col_idx[q];
-                const uint32_t pos = next[j]++;
-                if (pos >= p->csc_col_ptr[j + 1] || p->csc_row_idx[pos] != (uint32_t)i ||
-                    p->csc_val[pos] != p->csr_val[q])
-                    return bail(CDMF_ERR_INVALID);
-                to_csc[q] = pos;
-            }
+        uvec<uint32_t> to_csc(N);
+        if (h->relabeled) {
+            // both copies were built from the CSR: invert the CSC -> CSR map
+#pragma omp parallel for schedule(static)
+            for (int64_t o = 0; o < N; ++o) to_csc[h->csc_from_csr[o]] = (uint32_t)o;
+        } else {
+            std::vector<uint32_t> next(p->csc_col_ptr, p->csc_col_ptr + n);
+            for (int64_t i = 0; i < m; ++i)
+                for (uint32_t q = p->csr_row_ptr[i]; q < p->csr_row_ptr[i + 1]; ++q) {
+                    const uint32_t j = p->csr_col_idx[q];
+                    const uint32_t pos = next[j]++;
+                    if (pos >= p->csc_col_ptr[j + 1] || p->csc_row_idx[pos] != (uint32_t)i ||
+                        p->csc_val[pos] != p->csr_val[q])
+                        return bail(CDMF_ERR_INVALID);
+                    to_csc[q] = pos;
+                }
+        }
         h->kp = (o->k + 3) / 4 * 4;
         const int64_t nchunks = (N + kRefreshChunk - 1) / kRefreshChunk;
         h->ref_grid = (int)std::max<int64_t>(1, std::min<int64_t>(152 * 8, nchunks));
@@ -1048,6 +1083,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
             return bail(r);
         if (h->blocked) {
             // the refresh writes both copies at their blocked positions
+#pragma omp parallel for schedule(static)
             for (int64_t q = 0; q < N; ++q) to_csc[q] = h->hmap_c[to_csc[q]];
             h->ref_to_csr = h->bcsr.map;
         }
@@ -1221,6 +1257,7 @@ int cdmf_cuda_get_state(cdmf_handle* h, float* W, float* H, float* res_csc, floa
         }
         return CDMF_OK;
     };
+    if ((r = need_csc_pos(h))) return r;
     std::vector<float> tc, tr, bc, bq;
     float* dc = res_csc;
     float* dr = res_csr;
@@ -1249,6 +1286,8 @@ int cdmf_cuda_set_state(cdmf_handle* h, const float* W, const float* H, const fl
     if (!h || !W || !H || next_oiter < 1) return CDMF_ERR_INVALID;
     if (h->nnz > 0 && (!res_csc || !res_csr)) return CDMF_ERR_INVALID;
     CU(h, cudaSetDevice(h->o.device));
+    int r0 = need_csc_pos(h);
+    if (r0) return r0;
     std::vector<float> tw, th, tc, tr;
     if (h->relabeled) {
         tw.resize((size_t)h->o.k * h->m);
