@@ -82,6 +82,9 @@ EXPORTS = {
                                        OUTER_CB, ctypes.c_void_p]),
     "cdmf_cuda_rmse_coo": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_int64, ctypes.c_int64, c_f32p, c_f32p,
                                           ctypes.c_int64, c_u32p, c_u32p, c_f64p, ctypes.c_int, c_f64p, c_i64p]),
+    "cdmf_cuda_rmse_coo_noalloc": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p, c_f64p, c_i64p]),
     "cdmf_cuda_create": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Opts),
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "cdmf_cuda_destroy": (None, [ctypes.c_void_p]),

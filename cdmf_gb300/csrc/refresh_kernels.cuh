@@ -24,7 +24,7 @@ constexpr int kRefreshPerThread = 8;
 constexpr int kRefreshChunk = kBlock * kRefreshPerThread;
 
 // X (k x len, feature-major) -> Y (len x kp, row-major, padded with zeros).
-__global__ void __launch_bounds__(kBlock) to_row_major_kernel(const float* __restrict__ X, float* __restrict__ Y,
+static __global__ void __launch_bounds__(kBlock) to_row_major_kernel(const float* __restrict__ X, float* __restrict__ Y,
                                                               uint32_t k, uint32_t kp, int64_t len) {
     __shared__ float tile[32][33];
     const int64_t i0 = (int64_t)blockIdx.x * 32;

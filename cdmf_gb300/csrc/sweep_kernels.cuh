@@ -480,7 +480,7 @@ __global__ void CDMF_SWEEP_BOUNDS grouped_sweep_kernel(const SweepArgs* __restri
 
 // P[i] = (prev[i] or 0, cur[i]): the packed CSC table when no sweep has
 // written it (start of a run, after a state change).
-__global__ void pack_p_kernel(float2* __restrict__ P, const float* __restrict__ prev, const float* __restrict__ cur,
+static __global__ void pack_p_kernel(float2* __restrict__ P, const float* __restrict__ prev, const float* __restrict__ cur,
                               int64_t len) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
         P[i] = make_float2(prev ? prev[i] : 0.0f, cur[i]);

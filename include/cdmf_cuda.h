@@ -146,6 +146,26 @@ int cdmf_cuda_rmse_coo(uint32_t k, int64_t m, int64_t n, const float* W, const f
                        const uint32_t* test_row, const uint32_t* test_col, const double* test_val, int device,
                        double* rmse, int64_t* nan_count);
 
+/* Test RMSE on device arrays without any allocation by the library.  It has
+ * no counterpart in the reference.  For callers that cannot let a library
+ * call cudaMalloc (a process whose device memory all comes from its own pool,
+ * work recorded into a stream capture, a runtime with a fixed memory
+ * budget): W (k x m), H (k x n), test_row/test_col/test_val (nnz_test) are
+ * DEVICE pointers the caller owns, indices 0-based and in range; rmse and
+ * nan_count are host pointers.  Same arithmetic and result as
+ * cdmf_cuda_rmse_coo.  The kernel's scratch is a fixed file-scope device
+ * array of about 5 KB (608 block partials and three counters), held by every
+ * device that loads the library until exit and shared by all calls: calls
+ * that overlap on the GPU race on it.  The first call on a device looks up
+ * the array's address and should come before any stream capture.  Test sets
+ * larger than CDMF_NOALLOC_MAX_TEST entries (the reference counts entries in
+ * an int) are rejected with CDMF_ERR_TOO_LARGE.  stream: a cudaStream_t, or
+ * NULL for the default stream; the call waits for its own work. */
+#define CDMF_NOALLOC_MAX_TEST 2147483647LL
+int cdmf_cuda_rmse_coo_noalloc(uint32_t k, int64_t m, int64_t n, const float* W, const float* H, int64_t nnz_test,
+                               const uint32_t* test_row, const uint32_t* test_col, const double* test_val,
+                               void* stream, double* rmse, int64_t* nan_count);
+
 /* Handle API: the same engine split into upload / run / read-back. */
 int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** out);
 void cdmf_cuda_destroy(cdmf_handle* h);
