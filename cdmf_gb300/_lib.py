@@ -93,6 +93,7 @@ EXPORTS = {
     "cdmf_cuda_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_f64p]),
     "cdmf_cuda_get_factors": (ctypes.c_int, [ctypes.c_void_p, c_f32p, c_f32p]),
     "cdmf_cuda_rmse": (ctypes.c_int, [ctypes.c_void_p, c_f64p]),
+    "cdmf_cuda_objective": (ctypes.c_int, [ctypes.c_void_p, c_f64p, c_f64p, c_f64p]),
     "cdmf_cuda_get_state": (ctypes.c_int, [ctypes.c_void_p, c_f32p, c_f32p, c_f32p, c_f32p,
                                            ctypes.POINTER(ctypes.c_int)]),
     "cdmf_cuda_set_state": (ctypes.c_int, [ctypes.c_void_p, c_f32p, c_f32p, c_f32p, c_f32p, ctypes.c_int]),

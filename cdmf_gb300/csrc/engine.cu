@@ -20,6 +20,7 @@
 #include <cdmf_cuda.h>
 #include "sweep_kernels.cuh"
 #include "refresh_kernels.cuh"
+#include "objective_kernels.cuh"
 #include "tile_kernels.cuh"
 #include "blocked_kernels.cuh"
 #include "relabel.h"
@@ -181,6 +182,9 @@ struct cdmf_handle {
     uint32_t* ref_count = nullptr;
     unsigned long long* nonfinite = nullptr;
     bool refreshed = false;
+    // FP64 objective monitor (allocated on first use)
+    double *obj_part = nullptr, *obj_out = nullptr;
+    uint32_t* obj_count = nullptr;
     // CUDA graphs of whole outer iterations, keyed by the schedule's signature
     struct Graph {
         int sig[5];
@@ -696,6 +700,29 @@ int flush_pending(cdmf_handle* h) {
     return CDMF_OK;
 }
 
+template <int RT, int NU>
+void launch_refresh_t(cdmf_handle* h, const float* pa, const float* pb) {
+    refresh_warp_kernel<RT, NU><<<h->ref_grid, kBlock, 0, h->s>>>(
+        h->csr_ptr, h->csr_idx, h->csr_val, h->ref_to_csr, h->to_csc, h->m, h->nnz, h->Wrm, h->Hrm, h->kp,
+        h->res_csr, h->res_csc, pa, pb, h->ref_part, h->ref_count, h->drift_out, h->nonfinite);
+}
+
+template <int RT>
+void launch_refresh_rt(cdmf_handle* h, int nu, const float* pa, const float* pb) {
+    switch (nu) {
+        case 1: launch_refresh_t<RT, 1>(h, pa, pb); break;
+        case 2: launch_refresh_t<RT, 2>(h, pa, pb); break;
+        case 4: launch_refresh_t<RT, 4>(h, pa, pb); break;
+        case 8: launch_refresh_t<RT, 8>(h, pa, pb); break;
+        default: launch_refresh_t<RT, 0>(h, pa, pb); break;
+    }
+}
+
+void launch_refresh(cdmf_handle* h, int rt, int nu, const float* pa, const float* pb) {
+    if (rt == 1) launch_refresh_rt<1>(h, nu, pa, pb);
+    else launch_refresh_rt<2>(h, nu, pa, pb);
+}
+
 // 16-bit modes: recompute both residual copies from the FP32 ratings and
 // factors (clears the pending subtract).
 int refresh_residual(cdmf_handle* h) {
@@ -707,16 +734,9 @@ int refresh_residual(cdmf_handle* h) {
         dim3 gw((unsigned)((h->m + 31) / 32), (h->kp + 31) / 32), gh((unsigned)((h->n + 31) / 32), (h->kp + 31) / 32);
         if (h->m) to_row_major_kernel<<<gw, kBlock, 0, h->s>>>(h->W, h->Wrm, h->o.k, h->kp, h->m);
         if (h->n) to_row_major_kernel<<<gh, kBlock, 0, h->s>>>(h->H, h->Hrm, h->o.k, h->kp, h->n);
-        if (h->rt == 1)
-            refresh_kernel<1><<<h->ref_grid, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->csr_val, h->ref_to_csr, h->to_csc, h->m,
-                                                               h->nnz, h->Wrm, h->Hrm, h->kp, h->res_csr, h->res_csc,
-                                                               pa, pb, h->ref_part, h->ref_count, h->drift_out,
-                                                               h->nonfinite);
-        else
-            refresh_kernel<2><<<h->ref_grid, kBlock, 0, h->s>>>(h->csr_ptr, h->csr_idx, h->csr_val, h->ref_to_csr, h->to_csc, h->m,
-                                                               h->nnz, h->Wrm, h->Hrm, h->kp, h->res_csr, h->res_csc,
-                                                               pa, pb, h->ref_part, h->ref_count, h->drift_out,
-                                                               h->nonfinite);
+        const uint32_t kq = h->kp / 4;
+        const int nu = kq <= kRefG ? 1 : kq <= 2 * kRefG ? 2 : kq <= 4 * kRefG ? 4 : kq <= 8 * kRefG ? 8 : 0;
+        launch_refresh(h, h->rt, nu, pa, pb);
     }
     CU(h, cudaGetLastError());
     h->st.launches += 3;
@@ -1234,6 +1254,46 @@ int cdmf_cuda_rmse(cdmf_handle* h, double* rmse) {
     if (r) return r;
     CU(h, cudaMemcpyAsync(rmse, h->rmse_out, sizeof(double), cudaMemcpyDeviceToHost, h->s));
     CU(h, cudaStreamSynchronize(h->s));
+    return CDMF_OK;
+}
+
+int cdmf_cuda_objective(cdmf_handle* h, double* sq_residual, double* regularizer, double* objective) {
+    if (!h) return CDMF_ERR_INVALID;
+    CU(h, cudaSetDevice(h->o.device));
+    int r = flush_pending(h);
+    if (r) return r;
+    constexpr int kObjGrid = 4 * 152;
+    if (!h->obj_part) {
+        if ((r = dalloc(h, &h->obj_part, 3 * kObjGrid)) || (r = dalloc(h, &h->obj_out, 3)) ||
+            (r = dalloc(h, &h->obj_count, 1)))
+            return r;
+        CU(h, cudaMemsetAsync(h->obj_count, 0, sizeof(uint32_t), h->s));
+    }
+    const int64_t work = std::max<int64_t>(h->nnz, std::max(h->m, h->n));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(kObjGrid, (work + kBlock - 1) / kBlock));
+    switch (h->rt) {
+        case 0:
+            objective_kernel<0><<<grid, kBlock, 0, h->s>>>(h->res_csr, h->nnz, h->csr_ptr, h->m, h->csc_ptr, h->n, h->W,
+                                                           h->H, h->o.k, h->obj_part, h->obj_count, h->obj_out);
+            break;
+        case 1:
+            objective_kernel<1><<<grid, kBlock, 0, h->s>>>(h->res_csr, h->nnz, h->csr_ptr, h->m, h->csc_ptr, h->n, h->W,
+                                                           h->H, h->o.k, h->obj_part, h->obj_count, h->obj_out);
+            break;
+        default:
+            objective_kernel<2><<<grid, kBlock, 0, h->s>>>(h->res_csr, h->nnz, h->csr_ptr, h->m, h->csc_ptr, h->n, h->W,
+                                                           h->H, h->o.k, h->obj_part, h->obj_count, h->obj_out);
+            break;
+    }
+    CU(h, cudaGetLastError());
+    h->st.launches++;
+    double o[3];
+    CU(h, cudaMemcpyAsync(o, h->obj_out, sizeof(o), cudaMemcpyDeviceToHost, h->s));
+    CU(h, cudaStreamSynchronize(h->s));
+    const double reg = (double)h->o.lambda * (o[1] + o[2]);
+    if (sq_residual) *sq_residual = o[0];
+    if (regularizer) *regularizer = reg;
+    if (objective) *objective = o[0] + reg;
     return CDMF_OK;
 }
 

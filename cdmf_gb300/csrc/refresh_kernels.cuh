@@ -10,9 +10,11 @@
 // scattered to the CSC copy through the CSR->CSC position map.  The
 // scatter is L2-friendly: rows are visited in increasing order, so the
 // writes into a column's segment advance monotonically and partial sectors
-// merge in L2.  The same pass measures, in FP64, how far the stored residual
-// had drifted from the exact one (the residual-drift check) and counts
-// non-finite results.
+// merge in L2.  The same pass measures how far the stored residual had
+// drifted from the exact one (the residual-drift check: squares summed in
+// FP32 over at most 8 terms per lane, then in FP64) and counts non-finite
+// results.  The pass is bound by the gathers of factor rows from L2 (k * 8
+// bytes per nonzero), not by DRAM.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -43,14 +45,37 @@ static __global__ void __launch_bounds__(kBlock) to_row_major_kernel(const float
     }
 }
 
-template <int RT>
-__global__ void __launch_bounds__(kBlock) refresh_kernel(
+// Lane-group refresh.  Each warp owns runs of 32 consecutive CSR nonzeros;
+// lane l loads the index, rating and row of nonzero l (coalesced).  The dot
+// products W_i . H_j then run on groups of kRefG = 4 lanes: in each of four
+// rounds the eight groups take eight of the 32 nonzeros, and each lane reads
+// S 16-byte slices of the W row and of the H row (64 contiguous bytes per
+// group and slice: whole sectors), all independent loads in flight at once.
+// Two xor steps finish each sum and one shuffle hands it to the lane that
+// owns the nonzero, which then writes both residual copies.  S = float4
+// slices per lane (k <= 16, 32, 64, 128 -> S = 1, 2, 4, 8); S = 0 walks any
+// k.  Products are summed in a fixed order: deterministic.
+constexpr int kRefG = 4;
+#ifndef CDMF_REFRESH_UNROLL
+#define CDMF_REFRESH_UNROLL 2   // rounds whose loads are in flight together (measured: 2 > 1, 4 = 2)
+#endif
+#define CDMF_PRAGMA_(x) _Pragma(#x)
+#define CDMF_PRAGMA(x) CDMF_PRAGMA_(x)
+
+template <int RT, int S>
+__global__ void __launch_bounds__(kBlock) refresh_warp_kernel(
     const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ idx, const float* __restrict__ val,
-    const uint32_t* __restrict__ to_csr, const uint32_t* __restrict__ to_csc, int64_t m, int64_t nnz, const float* __restrict__ Wrm,
-    const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr, void* __restrict__ res_csc,
-    const float* __restrict__ pa, const float* __restrict__ pb_,  // pending subtract: a = H[tp] (cols), b = W[tp] (rows)
-    double* part, uint32_t* counter, double* drift_out, unsigned long long* nonfinite_out) {
+    const uint32_t* __restrict__ to_csr, const uint32_t* __restrict__ to_csc, int64_t m, int64_t nnz,
+    const float* __restrict__ Wrm, const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr,
+    void* __restrict__ res_csc, const float* __restrict__ pa, const float* __restrict__ pb_, double* part,
+    uint32_t* counter, double* drift_out, unsigned long long* nonfinite_out) {
     __shared__ uint32_t srow[2];
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr int kPer = 32 / kRefG;   // nonzeros per round
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gl = lane % kRefG, gi = lane / kRefG;
+    const int my_round = lane / kPer, my_src = (lane % kPer) * kRefG;
+    const uint32_t kq = kp / 4;   // float4 slices of a factor row (zero-padded past k)
     double drift = 0.0;
     unsigned bad = 0;
     const int64_t nchunks = (nnz + kRefreshChunk - 1) / kRefreshChunk;
@@ -58,7 +83,6 @@ __global__ void __launch_bounds__(kBlock) refresh_kernel(
         const int64_t p0 = c * kRefreshChunk;
         const int64_t p1 = (p0 + kRefreshChunk < nnz) ? p0 + kRefreshChunk : nnz;
         if (threadIdx.x < 2) {
-            // row containing p0 (thread 0) and p1 - 1 (thread 1): last row with ptr[row] <= p
             const int64_t p = threadIdx.x == 0 ? p0 : p1 - 1;
             int64_t lo = 0, hi = m;   // ptr[lo] <= p < ptr[hi]
             while (hi - lo > 1) {
@@ -69,57 +93,91 @@ __global__ void __launch_bounds__(kBlock) refresh_kernel(
         }
         __syncthreads();
         const uint32_t rlo = srow[0], rhi = srow[1];
-        // each thread takes kRefreshPerThread consecutive nonzeros: one
-        // binary search for the first, then the row advances by walking
-        const int64_t pb = p0 + (int64_t)threadIdx.x * kRefreshPerThread;
-        uint32_t i = rlo, bound = 0;
-        if (pb < p1) {
-            uint32_t lo = rlo, hi = rhi + 1;
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if ((int64_t)__ldg(ptr + mid) <= pb) lo = mid; else hi = mid;
+        float dsq = 0.0f;   // this chunk's squared drift (at most kRefreshPerThread terms per lane)
+        for (int s = 0; s < kRefreshPerThread; ++s) {
+            const int64_t base = p0 + ((int64_t)warp * kRefreshPerThread + s) * 32;
+            if (base >= p1) break;   // warp-uniform
+            const int cnt = (int)((p1 - base) < 32 ? (p1 - base) : 32);
+            const int64_t p = base + lane;
+            // lanes past the end keep row 0 and column 0 (both exist when
+            // nnz > 0): their products are computed and discarded
+            uint32_t i = 0, j = 0;
+            float v = 0.0f;
+            if (lane < cnt) {
+                uint32_t lo = rlo, hi = rhi + 1;   // ptr[lo] <= p < ptr[hi]
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if ((int64_t)__ldg(ptr + mid) <= p) lo = mid; else hi = mid;
+                }
+                i = lo;
+                j = __ldg(idx + p);
+                v = __ldg(val + p);
             }
-            i = lo;
-            bound = __ldg(ptr + i + 1);
-        }
-        for (int u = 0; u < kRefreshPerThread; ++u) {
-            const int64_t p = pb + u;
-            if (p >= p1) break;
-            while ((uint32_t)p >= bound) bound = __ldg(ptr + (++i) + 1);
-            const uint32_t j = __ldg(idx + p);
-            const float4* wr = (const float4*)(Wrm + (size_t)i * kp);
-            const float4* hr = (const float4*)(Hrm + (size_t)j * kp);
             float dot = 0.0f;
-            for (uint32_t q = 0; q < kp / 4; ++q) {
-                const float4 w = __ldg(wr + q), h = __ldg(hr + q);
-                dot = fmaf(w.x, h.x, dot);
-                dot = fmaf(w.y, h.y, dot);
-                dot = fmaf(w.z, h.z, dot);
-                dot = fmaf(w.w, h.w, dot);
+            CDMF_PRAGMA(unroll CDMF_REFRESH_UNROLL)
+            for (int r = 0; r < kRefG; ++r) {
+                const int src = r * kPer + gi;
+                const uint32_t ii = __shfl_sync(FULL, i, src);
+                const uint32_t jj = __shfl_sync(FULL, j, src);
+                const float4* wr = (const float4*)(Wrm + (size_t)ii * kp);
+                const float4* hr = (const float4*)(Hrm + (size_t)jj * kp);
+                float acc = 0.0f;
+                if (S > 0) {
+                    constexpr int SN = S > 0 ? S : 1;
+                    float4 w[SN], h[SN];
+#pragma unroll
+                    for (int u = 0; u < SN; ++u) {
+                        const uint32_t cq = gl + kRefG * u;
+                        w[u] = cq < kq ? __ldg(wr + cq) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        h[u] = cq < kq ? __ldg(hr + cq) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int u = 0; u < SN; ++u) {
+                        acc = fmaf(w[u].x, h[u].x, acc);
+                        acc = fmaf(w[u].y, h[u].y, acc);
+                        acc = fmaf(w[u].z, h[u].z, acc);
+                        acc = fmaf(w[u].w, h[u].w, acc);
+                    }
+                } else {
+                    for (uint32_t cq = gl; cq < kq; cq += kRefG) {
+                        const float4 w = __ldg(wr + cq), h = __ldg(hr + cq);
+                        acc = fmaf(w.x, h.x, acc);
+                        acc = fmaf(w.y, h.y, acc);
+                        acc = fmaf(w.z, h.z, acc);
+                        acc = fmaf(w.w, h.w, acc);
+                    }
+                }
+                acc = __fadd_rn(acc, __shfl_xor_sync(FULL, acc, 1));
+                acc = __fadd_rn(acc, __shfl_xor_sync(FULL, acc, 2));
+                const float got = __shfl_sync(FULL, acc, my_src);
+                if (my_round == r) dot = got;
             }
-            const float rnew = __fsub_rn(__ldg(val + p), dot);
-            const uint32_t pr = to_csr ? __ldg(to_csr + p) : (uint32_t)p;
-            float rold = Res<RT>::ld(res_csr, pr);
-            if (pa) rold = __fsub_rn(rold, __fmul_rn(__ldg(pa + j), __ldg(pb_ + i)));
-            const float stored = Res<RT>::st(res_csr, pr, rnew);
-            Res<RT>::st(res_csc, __ldg(to_csc + p), rnew);
-            if (!isfinite(stored)) bad++;
-            const double d = (double)rnew - (double)rold;
-            drift = __dadd_rn(drift, __dmul_rn(d, d));
+            if (lane < cnt) {
+                const float rnew = __fsub_rn(v, dot);
+                const uint32_t pr = to_csr ? __ldg(to_csr + p) : (uint32_t)p;
+                float rold = Res<RT>::ld(res_csr, pr);
+                if (pa) rold = __fsub_rn(rold, __fmul_rn(__ldg(pa + j), __ldg(pb_ + i)));
+                const float stored = Res<RT>::st(res_csr, pr, rnew);
+                Res<RT>::st(res_csc, __ldg(to_csc + p), rnew);
+                if (!isfinite(stored)) bad++;
+                const float d = __fsub_rn(rnew, rold);
+                dsq = __fadd_rn(dsq, __fmul_rn(d, d));
+            }
         }
+        drift = __dadd_rn(drift, (double)dsq);
         __syncthreads();
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        drift = __dadd_rn(drift, __shfl_xor_sync(0xffffffffu, drift, o));
-        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+        drift = __dadd_rn(drift, __shfl_xor_sync(FULL, drift, o));
+        bad += __shfl_xor_sync(FULL, bad, o);
     }
     __shared__ double sm[kWarps];
     __shared__ unsigned smb[kWarps];
     __shared__ int last;
-    if ((threadIdx.x & 31) == 0) {
-        sm[threadIdx.x >> 5] = drift;
-        smb[threadIdx.x >> 5] = bad;
+    if (lane == 0) {
+        sm[warp] = drift;
+        smb[warp] = bad;
     }
     __syncthreads();
     if (threadIdx.x == 0) {

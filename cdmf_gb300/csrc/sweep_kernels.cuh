@@ -95,14 +95,49 @@ struct SweepArgs {
     uint32_t* xcount;              // split-line arrival counters (left at 0)
 };
 
+// ---- streaming loads -----------------------------------------------------------
+// 128-bit and 64-bit loads of the index and residual streams, evict-first
+// (read once per sweep).  CDMF_STREAM_PF = 128 or 256 adds the L2 prefetch-size
+// hint, so an L2 miss fetches that many bytes from DRAM: the next chunk of a
+// lane's stream is on its way before the lane asks for it.
+#ifndef CDMF_STREAM_PF
+#define CDMF_STREAM_PF 256   // measured: +0.9 % FP32 updates/s, neutral at BF16
+#endif
+__device__ __forceinline__ uint4 ld_stream4(const void* p) {
+#if CDMF_STREAM_PF == 256
+    uint4 v;
+    asm("ld.global.cs.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+#elif CDMF_STREAM_PF == 128
+    uint4 v;
+    asm("ld.global.cs.L2::128B.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+#else
+    return __ldcs((const uint4*)p);
+#endif
+}
+__device__ __forceinline__ uint2 ld_stream2(const void* p) {
+#if CDMF_STREAM_PF == 256
+    uint2 v;
+    asm("ld.global.cs.L2::256B.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+#elif CDMF_STREAM_PF == 128
+    uint2 v;
+    asm("ld.global.cs.L2::128B.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+#else
+    return __ldcs((const uint2*)p);
+#endif
+}
+
 // ---- residual element access -------------------------------------------------
 template <int RT> struct Res;
 template <> struct Res<0> {
     static __device__ __forceinline__ float ld(const void* p, uint32_t q) { return __ldcs((const float*)p + q); }
     static __device__ __forceinline__ float st(void* p, uint32_t q, float v) { __stcs((float*)p + q, v); return v; }
     static __device__ __forceinline__ void ld4(const void* p, uint32_t q, float (&r)[4]) {
-        const float4 v = __ldcs((const float4*)((const float*)p + q));
-        r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+        const uint4 v = ld_stream4((const float*)p + q);
+        r[0] = __uint_as_float(v.x); r[1] = __uint_as_float(v.y); r[2] = __uint_as_float(v.z); r[3] = __uint_as_float(v.w);
     }
     static __device__ __forceinline__ void st4(void* p, uint32_t q, float (&r)[4]) {
         __stcs((float4*)((float*)p + q), make_float4(r[0], r[1], r[2], r[3]));
@@ -132,7 +167,7 @@ template <int KIND> struct Res16 {
         return rv;
     }
     static __device__ __forceinline__ void ld4(const void* p, uint32_t q, float (&r)[4]) {
-        const uint2 v = __ldcs((const uint2*)((const unsigned short*)p + q));
+        const uint2 v = ld_stream2((const unsigned short*)p + q);
         r[0] = to_f((unsigned short)(v.x & 0xffff));
         r[1] = to_f((unsigned short)(v.x >> 16));
         r[2] = to_f((unsigned short)(v.y & 0xffff));
@@ -239,7 +274,7 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
         float r[kChunks][4];
 #pragma unroll
         for (int u = 0; u < kChunks; ++u) {
-            const uint4 v = __ldcs((const uint4*)(A.idx + q + 4u * S * u));
+            const uint4 v = ld_stream4(A.idx + q + 4u * S * u);
             iv[u][0] = v.x; iv[u][1] = v.y; iv[u][2] = v.z; iv[u][3] = v.w;
             Res<RT>::ld4(A.res, q + 4u * S * u, r[u]);
         }
@@ -258,7 +293,7 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
         }
     }
     for (; q < vend; q += 4u * S) {
-        const uint4 v = __ldcs((const uint4*)(A.idx + q));
+        const uint4 v = ld_stream4(A.idx + q);
         const uint32_t iv[4] = {v.x, v.y, v.z, v.w};
         float r[4], y[4];
         Res<RT>::ld4(A.res, q, r);

@@ -121,6 +121,13 @@ class Engine:
         check(self.lib.cdmf_cuda_rmse(self.h, ctypes.byref(r)), "cdmf_cuda_rmse", self.h)
         return r.value
 
+    def objective(self):
+        """(sum of squared residuals, lambda-weighted regulariser, their sum), FP64."""
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(self.lib.cdmf_cuda_objective(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+              "cdmf_cuda_objective", self.h)
+        return a.value, b.value, c.value
+
     def state(self):
         W = np.empty((self.k, self.R.m), np.float32)
         H = np.empty((self.k, self.R.n), np.float32)

@@ -179,6 +179,13 @@ int cdmf_cuda_run(cdmf_handle* h, int n_outer, double* rmse_out);
 int cdmf_cuda_get_factors(cdmf_handle* h, float* W, float* H);
 /* Test RMSE of the current factors (src/tools.cpp:543-582). */
 int cdmf_cuda_rmse(cdmf_handle* h, double* rmse);
+/* FP64 training objective of the current state, a convergence monitor:
+ * sq_residual = sum of r_ij^2 over the training nonzeros (the `loss` that
+ * UpdateRating computes and discards, src/cdmf_ref.cpp:20-43), regularizer =
+ * lambda * (sum_i nnz_i |w_i|^2 + sum_j nnz_j |h_j|^2) (the lambda scaling of
+ * RankOneUpdate, src/cdmf_ref.cpp:7-17), objective = their sum.  Any output
+ * may be NULL.  Applies a deferred subtract first, as get_state does. */
+int cdmf_cuda_objective(cdmf_handle* h, double* sq_residual, double* regularizer, double* objective);
 /* Full engine state for one-step parity: factors, both residual copies (in
  * CSC and CSR order, widened to float) and the next outer iteration number. */
 int cdmf_cuda_get_state(cdmf_handle* h, float* W, float* H, float* res_csc, float* res_csr, int* next_oiter);

@@ -105,6 +105,24 @@ def rmse(R, W, H, k):
     return lib.oracle_rmse(ctypes.byref(P), k, _p(W), _p(H))
 
 
+def objective(R, W, H, res, lam):
+    """FP64 objective of a state: (sum r^2, lambda (sum_i nnz_i |w_i|^2 + sum_j nnz_j |h_j|^2), total).
+
+    The first term is the loss that UpdateRating accumulates over the CSC copy
+    (src/cdmf_ref.cpp:20-43); the regulariser weights each line by its
+    nonzero count, as RankOneUpdate scales lambda (src/cdmf_ref.cpp:8).
+    """
+    r = np.asarray(res, np.float64)
+    sq = float(np.dot(r, r))
+    nr = np.diff(R.csr_ptr.astype(np.int64)).astype(np.float64)
+    nc = np.diff(R.csc_ptr.astype(np.int64)).astype(np.float64)
+    W64 = np.asarray(W, np.float64)
+    H64 = np.asarray(H, np.float64)
+    lam = float(np.float32(lam))   # parameter.lambda is a VALUE_TYPE float (src/pmf.h:16)
+    reg = lam * (float(np.dot(nr, (W64 * W64).sum(axis=0))) + float(np.dot(nc, (H64 * H64).sum(axis=0))))
+    return sq, reg, sq + reg
+
+
 def reference_available():
     return os.path.exists(REF_LIB)
 

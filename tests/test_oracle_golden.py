@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, load_golden
+from cdmf_gb300 import formats
 from oracle import oracle
 
 META = json.load(open(os.path.join(GOLDEN, "golden.json")))
@@ -84,3 +85,19 @@ def test_fp64_oracle_tracks_fp32():
                      dtype=np.float64)
     assert np.max(np.abs(a["rmse"] - b["rmse"])) < 1e-4
     assert np.max(np.abs(a["W"] - b["W"])) < 1e-3 * np.max(np.abs(b["W"]))
+
+
+def test_oracle_objective_hand_case():
+    """2 x 2 ratings [[1, 0], [2, 3]] (3 nonzeros), k = 1: the FP64 objective
+    by hand: residual squares plus lambda times count-weighted factor norms."""
+    e = np.zeros(0, np.uint32)
+    R = formats.from_coo(2, 2, np.array([0, 1, 1]), np.array([0, 0, 1]), np.array([1.0, 2.0, 3.0], np.float32),
+                         e, e, np.zeros(0, np.float32))
+    W = np.array([[0.5, 2.0]], np.float32)
+    H = np.array([[1.0, -1.0]], np.float32)
+    res = np.array([0.25, -0.5, 1.0], np.float32)
+    sq, reg, tot = oracle.objective(R, W, H, res, 0.5)
+    assert sq == pytest.approx(0.0625 + 0.25 + 1.0, abs=1e-15)
+    # rows: nnz 1 and 2; columns: nnz 2 and 1
+    assert reg == pytest.approx(0.5 * (1 * 0.25 + 2 * 4.0 + 2 * 1.0 + 1 * 1.0), abs=1e-15)
+    assert tot == pytest.approx(sq + reg, abs=1e-15)
