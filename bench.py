@@ -133,13 +133,18 @@ def measured_peak():
 
 def profiled_traffic():
     """DRAM bytes per sweep launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "sweep_traffic.json")
-    if os.path.exists(path):
-        try:
-            return json.load(open(path))
-        except Exception:
-            return None
-    return None
+    path = os.path.join(ROOT, "profiles", "sweep_kernel_netflix_bf16.md")
+    if not os.path.exists(path):
+        return None
+    out = {}
+    for line in open(path):
+        for key in ("workload", "residual", "traffic_bytes_per_launch"):
+            if line.startswith(key + ":"):
+                out[key] = line.split(":", 1)[1].strip()
+    if "traffic_bytes_per_launch" not in out:
+        return None
+    return {"workload": out.get("workload"), "residual": out.get("residual"),
+            "dram_bytes_per_launch": int(out["traffic_bytes_per_launch"])}
 
 
 def cpu_sample(R, run, W0, threads, budget_s):
@@ -270,7 +275,8 @@ def main():
     peak, peak_kind = measured_peak()
     tr = profiled_traffic()
     traffic = None
-    if tr and tr.get("workload") == WORKLOAD and tr.get("residual") == args.residual:
+    if (tr and tr.get("workload") == WORKLOAD and tr.get("residual") == args.residual and args.version in (1, 2)
+            and args.layout == "lines" and args.k == 64):
         traffic = tr.get("dram_bytes_per_launch")
 
     if args.quick:
