@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp", "-I", INC]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-I", INC]
 
-CU_SOURCES = ["engine.cu", "noalloc.cu"]
+CU_SOURCES = ["engine.cu", "noalloc.cu", "compress.cu"]
 CXX_SOURCES = ["synth.cpp", "relabel.cpp", "blocked.cpp"]
 CLI_SOURCES = ["cli/main.cpp", "cli/loader.cpp"]
 

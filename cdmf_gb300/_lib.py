@@ -85,6 +85,17 @@ EXPORTS = {
     "cdmf_cuda_rmse_coo_noalloc": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                                   ctypes.c_void_p, ctypes.c_void_p, c_f64p, c_i64p]),
+    "cdmf_cuda_compress": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, c_u32p, c_u32p, c_f64p,
+                                          ctypes.c_int, c_u32p, c_u32p, c_f32p, c_u32p, c_u32p, c_f32p, c_i64p]),
+    "cdmf_spmv_create": (ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "cdmf_spmv_destroy": (None, [ctypes.c_void_p]),
+    "cdmf_spmv_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "cdmf_spmv_input_csr": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
+    "cdmf_spmv_as_csr5": (ctypes.c_int, [ctypes.c_void_p]),
+    "cdmf_spmv_as_csr": (ctypes.c_int, [ctypes.c_void_p]),
+    "cdmf_spmv_set_x": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "cdmf_spmv_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, c_f64p]),
     "cdmf_cuda_create": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(Opts),
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "cdmf_cuda_destroy": (None, [ctypes.c_void_p]),

@@ -1,0 +1,234 @@
+// COO -> canonical CSR and CSC on the GPU (cdmf_cuda_compress).
+//
+// The reference builds its binary CSR/CSC files offline with scipy
+// (data/a/a_compress.py:130-155: coo_matrix(...).tocsr() / .tocsc()) and the
+// engine loads them (src/tools.cpp:271-347).  This entry point produces the
+// same arrays from a COO rating list on the device:
+//   1. key = row * n + col (64-bit), checked against m and n;
+//   2. stable radix sort of (key, input position): entries in (row, col)
+//      order, equal keys in input order;
+//   3. one thread per distinct key sums its duplicates in FP64 in input order
+//      and stores the float value (scipy sums duplicates; the reference then
+//      writes float32);
+//   4. row pointers from the sorted keys;
+//   5. stable radix sort of the distinct entries by column gives the CSC
+//      order with rows ascending inside each column (scipy's canonical CSC)
+//      and the CSR -> CSC permutation.
+// The sorts are CUB's DeviceRadixSort (shipped with the CUDA toolkit); the
+// other steps are the kernels below.  Inputs and outputs are host arrays; the
+// device scratch is allocated per call and freed before it returns.
+#include <cdmf_cuda.h>
+
+#include <cub/cub.cuh>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+namespace {
+
+constexpr int kThreads = 256;
+
+unsigned grid_for(int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + kThreads - 1) / kThreads, 1 << 20)); }
+
+__global__ void make_keys(const uint32_t* __restrict__ rows, const uint32_t* __restrict__ cols, int64_t nnz, uint64_t m,
+                          uint64_t n, uint64_t* __restrict__ keys, uint32_t* __restrict__ pos, uint32_t* bad) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = rows[e], c = cols[e];
+        if (r >= m || c >= n) {
+            atomicOr(bad, 1u);
+            keys[e] = 0;
+        } else {
+            keys[e] = r * n + c;
+        }
+        pos[e] = (uint32_t)e;
+    }
+}
+
+// head[i] = 1 where a run of equal keys starts
+__global__ void run_heads(const uint64_t* __restrict__ keys, int64_t nnz, uint32_t* __restrict__ head) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x)
+        head[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+// start[uid[i]] = i at every run head; start[U] = nnz
+__global__ void run_starts(const uint32_t* __restrict__ head, const uint32_t* __restrict__ uid, int64_t nnz,
+                           uint32_t* __restrict__ start) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x) {
+        if (head[i]) start[uid[i]] = (uint32_t)i;
+        if (i == nnz - 1) start[uid[i] + head[i]] = (uint32_t)nnz;
+    }
+}
+
+// One distinct (row, col): duplicates summed in FP64 in input order.
+__global__ void reduce_runs(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ pos,
+                            const double* __restrict__ vals, const uint32_t* __restrict__ start, int64_t U, uint64_t n,
+                            uint32_t* __restrict__ row, uint32_t* __restrict__ col, float* __restrict__ val) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < U; u += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = start[u], e = start[u + 1];
+        double s = 0.0;
+        for (uint32_t i = b; i < e; ++i) s = __dadd_rn(s, vals[pos[i]]);
+        const uint64_t key = keys[b];
+        row[u] = (uint32_t)(key / n);
+        col[u] = (uint32_t)(key % n);
+        val[u] = __double2float_rn(s);
+    }
+}
+
+// ptr[l] = first position of line l in a line-sorted list of U entries
+// (lines with no entries point at the next line's first entry).
+__global__ void line_pointers(const uint32_t* __restrict__ line, int64_t U, int64_t lines, uint32_t* __restrict__ ptr) {
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < U; u += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t l = line[u];
+        const int64_t prev = u == 0 ? -1 : (int64_t)line[u - 1];
+        for (int64_t q = prev + 1; q <= l; ++q) ptr[q] = (uint32_t)u;
+        if (u == U - 1)
+            for (int64_t q = l + 1; q <= lines; ++q) ptr[q] = (uint32_t)U;
+    }
+}
+
+__global__ void gather_csc(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ row,
+                           const float* __restrict__ val, int64_t U, uint32_t* __restrict__ cidx, float* __restrict__ cval) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < U; v += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t u = perm[v];
+        cidx[v] = row[u];
+        cval[v] = val[u];
+    }
+}
+
+int bits_for(uint64_t maxval) {
+    int b = 1;
+    while (b < 64 && (maxval >> b) != 0) ++b;
+    return b;
+}
+
+// Device buffers of one call, freed on every return path.
+struct Scratch {
+    std::vector<void*> ptrs;
+    template <class T>
+    bool get(T** p, size_t count) {
+        *p = nullptr;
+        if (cudaMalloc((void**)p, std::max<size_t>(1, count) * sizeof(T)) != cudaSuccess) return false;
+        ptrs.push_back(*p);
+        return true;
+    }
+    ~Scratch() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+}  // namespace
+
+#define CC(x)                                  \
+    do {                                       \
+        if ((x) != cudaSuccess) {              \
+            cudaStreamSynchronize(s);          \
+            cudaStreamDestroy(s);              \
+            return CDMF_ERR_CUDA;              \
+        }                                      \
+    } while (0)
+#define CA(x)                                  \
+    do {                                       \
+        if (!(x)) {                            \
+            cudaStreamDestroy(s);              \
+            return CDMF_ERR_ALLOC;             \
+        }                                      \
+    } while (0)
+
+extern "C" int cdmf_cuda_compress(int64_t m, int64_t n, int64_t nnz, const uint32_t* rows, const uint32_t* cols,
+                                  const double* vals, int device, uint32_t* csr_ptr, uint32_t* csr_idx, float* csr_val,
+                                  uint32_t* csc_ptr, uint32_t* csc_idx, float* csc_val, int64_t* nnz_out) {
+    if (m < 0 || n < 0 || nnz < 0 || !csr_ptr || !csc_ptr || !nnz_out) return CDMF_ERR_INVALID;
+    if (nnz > 0 && (!rows || !cols || !vals || !csr_idx || !csr_val || !csc_idx || !csc_val || m == 0 || n == 0))
+        return CDMF_ERR_INVALID;
+    if (nnz > (int64_t)UINT32_MAX - 8192 || m >= (int64_t)UINT32_MAX || n >= (int64_t)UINT32_MAX)
+        return CDMF_ERR_TOO_LARGE;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CDMF_ERR_NO_DEVICE;
+    if (device < 0 || device >= ndev) return CDMF_ERR_NO_DEVICE;
+    if (cudaSetDevice(device) != cudaSuccess) return CDMF_ERR_CUDA;
+    *nnz_out = 0;
+    if (nnz == 0) {
+        std::fill(csr_ptr, csr_ptr + m + 1, 0u);
+        std::fill(csc_ptr, csc_ptr + n + 1, 0u);
+        return CDMF_OK;
+    }
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return CDMF_ERR_CUDA;
+    const size_t N = (size_t)nnz;
+    int64_t U = 0;
+    {
+        Scratch S;
+        uint32_t *d_rows, *d_cols, *pos_a, *pos_b, *head, *uid, *start, *row, *col, *cidx, *perm, *ccol,
+            *d_rptr, *d_cptr, *bad;
+        uint64_t *key_a, *key_b;
+        double* d_vals;
+        float *val, *cval;
+        CA(S.get(&d_rows, N) && S.get(&d_cols, N) && S.get(&d_vals, N) && S.get(&key_a, N) && S.get(&key_b, N) &&
+           S.get(&pos_a, N) && S.get(&pos_b, N) && S.get(&head, N) && S.get(&uid, N) && S.get(&start, N + 1) &&
+           S.get(&bad, 1));
+        CC(cudaMemcpyAsync(d_rows, rows, 4 * N, cudaMemcpyHostToDevice, s));
+        CC(cudaMemcpyAsync(d_cols, cols, 4 * N, cudaMemcpyHostToDevice, s));
+        CC(cudaMemcpyAsync(d_vals, vals, 8 * N, cudaMemcpyHostToDevice, s));
+        CC(cudaMemsetAsync(bad, 0, 4, s));
+        make_keys<<<grid_for(nnz), kThreads, 0, s>>>(d_rows, d_cols, nnz, (uint64_t)m, (uint64_t)n, key_a, pos_a, bad);
+        CC(cudaGetLastError());
+        uint32_t h_bad = 0;
+        CC(cudaMemcpyAsync(&h_bad, bad, 4, cudaMemcpyDeviceToHost, s));
+        CC(cudaStreamSynchronize(s));
+        if (h_bad) {
+            cudaStreamDestroy(s);
+            return CDMF_ERR_INVALID;
+        }
+        // 1. stable sort by (row, col)
+        const int kbits = bits_for((uint64_t)m * (uint64_t)n - 1);
+        size_t tmp_bytes = 0, t2 = 0, t3 = 0;
+        CC(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, key_a, key_b, pos_a, pos_b, nnz, 0, kbits, s));
+        CC(cub::DeviceScan::ExclusiveSum(nullptr, t2, head, uid, nnz, s));
+        const int cbits = bits_for((uint64_t)n - 1);
+        CC(cub::DeviceRadixSort::SortPairs(nullptr, t3, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                           (const uint32_t*)nullptr, (uint32_t*)nullptr, nnz, 0, cbits, s));
+        tmp_bytes = std::max(tmp_bytes, std::max(t2, t3));
+        char* tmp = nullptr;
+        CA(S.get(&tmp, tmp_bytes));
+        CC(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, key_a, key_b, pos_a, pos_b, nnz, 0, kbits, s));
+        // 2. runs of equal keys
+        run_heads<<<grid_for(nnz), kThreads, 0, s>>>(key_b, nnz, head);
+        CC(cudaGetLastError());
+        CC(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, head, uid, nnz, s));
+        run_starts<<<grid_for(nnz), kThreads, 0, s>>>(head, uid, nnz, start);
+        CC(cudaGetLastError());
+        uint32_t last_uid = 0, last_head = 0;
+        CC(cudaMemcpyAsync(&last_uid, uid + N - 1, 4, cudaMemcpyDeviceToHost, s));
+        CC(cudaMemcpyAsync(&last_head, head + N - 1, 4, cudaMemcpyDeviceToHost, s));
+        CC(cudaStreamSynchronize(s));
+        U = (int64_t)last_uid + last_head;
+        // 3. distinct entries in CSR order
+        CA(S.get(&row, U) && S.get(&col, U) && S.get(&val, U) && S.get(&d_rptr, m + 1) && S.get(&d_cptr, n + 1) &&
+           S.get(&perm, U) && S.get(&ccol, U) && S.get(&cidx, U) && S.get(&cval, U));
+        reduce_runs<<<grid_for(U), kThreads, 0, s>>>(key_b, pos_b, d_vals, start, U, (uint64_t)n, row, col, val);
+        CC(cudaGetLastError());
+        line_pointers<<<grid_for(U), kThreads, 0, s>>>(row, U, m, d_rptr);
+        CC(cudaGetLastError());
+        // 4. CSC: stable sort of the distinct entries by column; the values are
+        // their CSR positions (pos_a still holds 0..nnz-1: the first sort wrote
+        // its output to pos_b and left its input alone)
+        CC(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, col, ccol, pos_a, perm, U, 0, cbits, s));
+        gather_csc<<<grid_for(U), kThreads, 0, s>>>(perm, row, val, U, cidx, cval);
+        CC(cudaGetLastError());
+        line_pointers<<<grid_for(U), kThreads, 0, s>>>(ccol, U, n, d_cptr);
+        CC(cudaGetLastError());
+        // 5. results to the host
+        CC(cudaMemcpyAsync(csr_ptr, d_rptr, 4 * (size_t)(m + 1), cudaMemcpyDeviceToHost, s));
+        CC(cudaMemcpyAsync(csr_idx, col, 4 * (size_t)U, cudaMemcpyDeviceToHost, s));
+        CC(cudaMemcpyAsync(csr_val, val, 4 * (size_t)U, cudaMemcpyDeviceToHost, s));
+        CC(cudaMemcpyAsync(csc_ptr, d_cptr, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s));
+        CC(cudaMemcpyAsync(csc_idx, cidx, 4 * (size_t)U, cudaMemcpyDeviceToHost, s));
+        CC(cudaMemcpyAsync(csc_val, cval, 4 * (size_t)U, cudaMemcpyDeviceToHost, s));
+        CC(cudaStreamSynchronize(s));
+    }
+    cudaStreamDestroy(s);
+    *nnz_out = U;
+    return CDMF_OK;
+}

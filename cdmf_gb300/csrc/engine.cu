@@ -35,6 +35,7 @@
 #include <mutex>
 #include <tuple>
 #include <cstdio>
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -987,6 +988,15 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         p->nnz_test > (int64_t)INT32_MAX * 64)
         return CDMF_ERR_TOO_LARGE;
     int r;
+    // o->verbose: phase times of the set-up on stderr
+    auto t_last = std::chrono::steady_clock::now();
+    auto phase = [&](const char* what) {
+        if (!o->verbose) return;
+        const auto t = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[cdmf] create: %-12s %8.1f ms\n", what,
+                     std::chrono::duration<double, std::milli>(t - t_last).count());
+        t_last = t;
+    };
     if ((r = check_compressed(p->csr_row_ptr, p->csr_col_idx, p->m, p->n, p->nnz))) return r;
     if ((r = check_compressed(p->csc_col_ptr, p->csc_row_idx, p->n, p->m, p->nnz))) return r;
     if (p->nnz > 0 && (!p->csr_val || !p->csc_val)) return CDMF_ERR_INVALID;
@@ -995,6 +1005,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         for (int64_t e = 0; e < p->nnz_test; ++e)
             if ((int64_t)p->test_row[e] >= p->m || (int64_t)p->test_col[e] >= p->n) return CDMF_ERR_INVALID;
     }
+    phase("checks");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CDMF_ERR_NO_DEVICE;
     if (o->device < 0 || o->device >= ndev) return CDMF_ERR_NO_DEVICE;
@@ -1014,6 +1025,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         q.test_row = RL.te_row.data();
         q.test_col = RL.te_col.data();
         p = &q;
+        phase("relabel");
     }
     cdmf_handle* h = new cdmf_handle();
     if (p == &q) {
@@ -1024,6 +1036,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         h->csc_from_csr = std::move(RL.csc_from_csr);
         h->ucsr_ptr.assign(q0.csr_row_ptr, q0.csr_row_ptr + q0.m + 1);
         h->ucsr_idx.assign(q0.csr_col_idx, q0.csr_col_idx + q0.nnz);
+        phase("keep maps");
     }
     h->o = *o;
     h->m = p->m;
@@ -1063,6 +1076,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         (r = up(h->te_val, p->test_val, 4 * h->nt)))
         return bail(r);
     if (cudaMemsetAsync(h->rmse_count, 0, 4, h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    phase("alloc+upload");
     const bool seq = o->reduce == CDMF_REDUCE_SEQUENTIAL;
     h->blocked = o->layout == 1 && !seq && N > 0;
     if (h->blocked) {
@@ -1108,6 +1122,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
             h->ref_to_csr = h->bcsr.map;
         }
         if ((r = up(h->to_csc, to_csc.data(), 4 * N))) return bail(r);
+        phase("refresh map");
         if (cudaMemsetAsync(h->ref_count, 0, 4, h->s) != cudaSuccess ||
             cudaMemsetAsync(h->nonfinite, 0, 8, h->s) != cudaSuccess ||
             cudaMemsetAsync(h->drift_out, 0, 8, h->s) != cudaSuccess ||
@@ -1120,6 +1135,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if ((r = upload_bins(h, h->csr, plan_bins(p->csr_row_ptr, m, seq, h->cfg))) ||
         (r = upload_bins(h, h->csc, plan_bins(p->csc_col_ptr, n, seq, h->cfg))))
         return bail(r);
+    phase("bins");
     h->tiles = o->version == 3 && !seq && !h->blocked;
     if (h->tiles && ((r = upload_tiles(h, h->tcsr, p->csr_row_ptr, m, N)) ||
                      (r = upload_tiles(h, h->tcsc, p->csc_col_ptr, n, N))))
@@ -1131,6 +1147,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if ((r = reset_residual(h, h->res_csr, h->csr_val)) || (r = reset_residual(h, h->res_csc, h->csc_val)))
         return bail(r);
     if (cudaStreamSynchronize(h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    phase("state");
     if (o->autotune && (r = cdmf_cuda_autotune(h, nullptr, nullptr))) return bail(r);
     const double T = std::max(1, o->maxinneriter);
     const double br = (double)h->rbytes;
@@ -2021,6 +2038,165 @@ int cdmf_cuda_batch_get_factors(cdmf_batch* B, float* const* W, float* const* H)
 int cdmf_cuda_batch_stats(const cdmf_batch* B, cdmf_stats* s) {
     if (!B || !s) return CDMF_ERR_INVALID;
     *s = B->st;
+    return CDMF_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Dual SpMV front end: the anonymouslibHandle life cycle the reference's -V 3
+// engine drives (src/anonymouslib_opencl.h:11-26; src/cdmf_csr5.cpp:205-286):
+// create(m, n), inputCSR(nnz, ptr, idx, val), asCSR5(), setX(x), then
+// spmv(alpha, y_t, y_b) computing, for every row i,
+//     y_t[i] = sum_j val_ij * x[col_j]      y_b[i] = sum_j x[col_j]^2
+// (csr5_spmv.cl:135-147: the per-nonzero pair; alpha is accepted and, as in
+// that kernel, not applied).  The CSR5 tiles become the engine's line-length
+// bins over the same CSR arrays: split chunks, CTA, warp, 8-lane group and
+// thread lines, each summed in a fixed tree order (deterministic).  Arrays
+// are the caller's device memory, as cl_mem buffers are in the reference.
+// ============================================================================
+
+namespace {
+
+__global__ void check_cols_kernel(const uint32_t* __restrict__ idx, int64_t nnz, uint32_t n, uint32_t* bad) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x)
+        if (idx[q] >= n) atomicOr(bad, 1u);
+}
+
+}  // namespace
+
+struct cdmf_spmv {
+    cdmf_handle* h = nullptr;        // stream, bins, allocations, error text
+    const uint32_t* row_ptr = nullptr;
+    const uint32_t* col_idx = nullptr;
+    const float* val = nullptr;
+    const float* x = nullptr;
+    bool have_csr = false, csr5 = false;
+};
+
+extern "C" {
+
+int cdmf_spmv_create(int64_t m, int64_t n, int device, cdmf_spmv** out) {
+    if (!out) return CDMF_ERR_INVALID;
+    *out = nullptr;
+    if (m < 0 || n < 0) return CDMF_ERR_INVALID;
+    if (m >= (int64_t)UINT32_MAX || n >= (int64_t)UINT32_MAX) return CDMF_ERR_TOO_LARGE;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return CDMF_ERR_NO_DEVICE;
+    if (device < 0 || device >= ndev) return CDMF_ERR_NO_DEVICE;
+    if (cudaSetDevice(device) != cudaSuccess) return CDMF_ERR_CUDA;
+    cdmf_spmv* S = new cdmf_spmv();
+    S->h = new cdmf_handle();
+    cdmf_opts_default(&S->h->o);
+    S->h->o.device = device;
+    S->h->m = m;
+    S->h->n = n;
+    if (cudaStreamCreateWithFlags(&S->h->s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&S->h->ev_start) != cudaSuccess || cudaEventCreate(&S->h->ev_stop) != cudaSuccess) {
+        cdmf_cuda_destroy(S->h);
+        delete S;
+        return CDMF_ERR_CUDA;
+    }
+    *out = S;
+    return CDMF_OK;
+}
+
+void cdmf_spmv_destroy(cdmf_spmv* S) {
+    if (!S) return;
+    cdmf_cuda_destroy(S->h);
+    delete S;
+}
+
+const char* cdmf_spmv_last_error(const cdmf_spmv* S) { return S ? S->h->err.c_str() : ""; }
+
+int cdmf_spmv_input_csr(cdmf_spmv* S, int64_t nnz, const uint32_t* row_ptr, const uint32_t* col_idx,
+                        const float* val) {
+    if (!S || nnz < 0 || !row_ptr || (nnz > 0 && (!col_idx || !val))) return CDMF_ERR_INVALID;
+    if (nnz > (int64_t)UINT32_MAX - 8192) return CDMF_ERR_TOO_LARGE;
+    cdmf_handle* h = S->h;
+    CU(h, cudaSetDevice(h->o.device));
+    if (S->csr5) free_bins(h, h->csr);
+    S->csr5 = false;
+    // the row pointers are read back to plan the work and checked here: a
+    // malformed structure is refused before any kernel reads through it
+    h->hptr_r.resize(h->m + 1);
+    CU(h, cudaMemcpyAsync(h->hptr_r.data(), row_ptr, 4 * (size_t)(h->m + 1), cudaMemcpyDeviceToHost, h->s));
+    CU(h, cudaStreamSynchronize(h->s));
+    if (h->hptr_r[0] != 0 || (int64_t)h->hptr_r[h->m] != nnz) return fail(h, CDMF_ERR_INVALID, "row_ptr ends");
+    for (int64_t i = 0; i < h->m; ++i)
+        if (h->hptr_r[i + 1] < h->hptr_r[i]) return fail(h, CDMF_ERR_INVALID, "row_ptr not monotone");
+    h->nnz = nnz;
+    S->row_ptr = row_ptr;
+    S->col_idx = col_idx;
+    S->val = val;
+    S->have_csr = true;
+    return CDMF_OK;
+}
+
+int cdmf_spmv_as_csr5(cdmf_spmv* S) {
+    if (!S) return CDMF_ERR_INVALID;
+    cdmf_handle* h = S->h;
+    if (!S->have_csr) return fail(h, CDMF_ERR_INVALID, "no matrix: call cdmf_spmv_input_csr first");
+    if (S->csr5) return CDMF_OK;
+    CU(h, cudaSetDevice(h->o.device));
+    if (h->nnz > 0) {   // every column index must address x
+        uint32_t* bad = nullptr;
+        int r;
+        if ((r = dalloc(h, &bad, 1))) return r;
+        CU(h, cudaMemsetAsync(bad, 0, 4, h->s));
+        check_cols_kernel<<<1216, kBlock, 0, h->s>>>(S->col_idx, h->nnz, (uint32_t)h->n, bad);
+        CU(h, cudaGetLastError());
+        uint32_t hb = 0;
+        CU(h, cudaMemcpyAsync(&hb, bad, 4, cudaMemcpyDeviceToHost, h->s));
+        CU(h, cudaStreamSynchronize(h->s));
+        if (hb) return fail(h, CDMF_ERR_INVALID, "column index out of range");
+    }
+    const int r = upload_bins(h, h->csr, plan_bins(h->hptr_r.data(), h->m, false, h->cfg));
+    if (r) return r;
+    S->csr5 = true;
+    return CDMF_OK;
+}
+
+int cdmf_spmv_as_csr(cdmf_spmv* S) {
+    if (!S) return CDMF_ERR_INVALID;
+    if (S->csr5) {
+        CU(S->h, cudaSetDevice(S->h->o.device));
+        CU(S->h, cudaStreamSynchronize(S->h->s));
+        free_bins(S->h, S->h->csr);
+    }
+    S->csr5 = false;
+    return CDMF_OK;
+}
+
+int cdmf_spmv_set_x(cdmf_spmv* S, const float* x) {
+    if (!S || (!x && S->h->n > 0)) return CDMF_ERR_INVALID;
+    S->x = x;
+    return CDMF_OK;
+}
+
+int cdmf_spmv_run(cdmf_spmv* S, float alpha, float* y_t, float* y_b, double* ms) {
+    (void)alpha;
+    if (!S) return CDMF_ERR_INVALID;
+    cdmf_handle* h = S->h;
+    if (!S->csr5) return fail(h, CDMF_ERR_UNSUPPORTED, "the matrix is in CSR form: call cdmf_spmv_as_csr5");
+    if ((h->m > 0 && (!y_t || !y_b)) || (h->nnz > 0 && !S->x)) return CDMF_ERR_INVALID;
+    CU(h, cudaSetDevice(h->o.device));
+    SweepArgs A = base_args(h, h->csr, S->row_ptr, S->col_idx, (void*)S->val);
+    A.y = S->x;
+    A.out = y_t;
+    A.out2 = y_b;
+    const unsigned grid = h->csr.nx + h->csr.nc + h->csr.nwb + h->csr.ngb + h->csr.ntb;
+    CU(h, cudaEventRecord(h->ev_start, h->s));
+    if (grid) {
+        prefer_l1(sweep_kernel<0, M_DUAL, false, false>);
+        sweep_kernel<0, M_DUAL, false, false><<<grid, kBlock, 0, h->s>>>(A);
+        CU(h, cudaGetLastError());
+    }
+    CU(h, cudaEventRecord(h->ev_stop, h->s));
+    CU(h, cudaEventSynchronize(h->ev_stop));
+    float t = 0.0f;
+    CU(h, cudaEventElapsedTime(&t, h->ev_start, h->ev_stop));
+    if (ms) *ms = t;
     return CDMF_OK;
 }
 

@@ -62,6 +62,7 @@ constexpr int kWarps = kBlock / 32;
 constexpr int M_PLAIN = 0;  // inner iterations >= 2: y only, no residual writes
 constexpr int M_CSC = 1;    // first CSC sweep of a feature: P gathers, emits Q
 constexpr int M_CSR = 2;    // first CSR sweep of a feature: Q gathers
+constexpr int M_DUAL = 3;   // dual SpMV (CSR5-style front end): y gathers, raw sums out
 
 struct XTask {            // one chunk of a split line
     uint32_t line, beg, end, slot;
@@ -93,6 +94,7 @@ struct SweepArgs {
     uint32_t ngb;                  // blocks of the group bin (32 lines per block)
     float2* part;                  // split-line partials
     uint32_t* xcount;              // split-line arrival counters (left at 0)
+    float* out2;                   // M_DUAL: sum of y^2 per line (out gets the sum of y * r)
 };
 
 // ---- streaming loads -----------------------------------------------------------
@@ -380,6 +382,11 @@ __device__ __forceinline__ void write_line(const SweepArgs& A, uint32_t j, float
 template <int MODE>
 __device__ __forceinline__ void finish_line(const SweepArgs& A, uint32_t j, uint32_t len, float g, float h, float bj,
                                             float dj) {
+    if (MODE == M_DUAL) {
+        A.out[j] = g;
+        A.out2[j] = h;
+        return;
+    }
     const float lam = __fmul_rn(A.lambda, __uint2float_rn(len));
     write_line<MODE>(A, j, len == 0 ? 0.0f : __fdiv_rn(g, __fadd_rn(lam, h)), bj, dj);
 }
@@ -474,6 +481,13 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
     const uint32_t len = end - beg;
     float bj, dj;
     line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
+    if (MODE == M_DUAL) {
+        Acc<false> g, h;
+        for (uint32_t q = beg; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
+        A.out[j] = g.s;
+        A.out2[j] = h.s;
+        return;
+    }
     if (len == 0) {
         write_line<MODE>(A, j, 0.0f, bj, dj);
         return;

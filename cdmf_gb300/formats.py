@@ -92,6 +92,32 @@ def compress(m, n, rows, cols, vals):
     return (_u32(csr_ptr), _u32(c), _f32(summed), _u32(csc_ptr), _u32(r[corder]), _f32(summed[corder]))
 
 
+def compress_gpu(m, n, rows, cols, vals, device=0):
+    """compress() on the GPU through cdmf_cuda_compress: same arrays, bit for
+    bit (duplicates summed in FP64 in input order, stored as float)."""
+    import ctypes
+    from . import _lib
+    rows = np.ascontiguousarray(rows, dtype=np.uint32)
+    cols = np.ascontiguousarray(cols, dtype=np.uint32)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    nnz = rows.size
+    if cols.size != nnz or vals.size != nnz:
+        raise ValueError("rows, cols and vals differ in length")
+    csr_ptr = np.empty(m + 1, np.uint32)
+    csc_ptr = np.empty(n + 1, np.uint32)
+    csr_idx, csc_idx = np.empty(nnz, np.uint32), np.empty(nnz, np.uint32)
+    csr_val, csc_val = np.empty(nnz, np.float32), np.empty(nnz, np.float32)
+    out = ctypes.c_int64()
+    U32, F32, F64 = ctypes.c_uint32, ctypes.c_float, ctypes.c_double
+    p = _lib.ptr
+    _lib.check(_lib.load().cdmf_cuda_compress(m, n, nnz, p(rows, U32), p(cols, U32), p(vals, F64), device,
+                                              p(csr_ptr, U32), p(csr_idx, U32), p(csr_val, F32), p(csc_ptr, U32),
+                                              p(csc_idx, U32), p(csc_val, F32), ctypes.byref(out)),
+               "cdmf_cuda_compress")
+    u = out.value
+    return csr_ptr, csr_idx[:u].copy(), csr_val[:u].copy(), csc_ptr, csc_idx[:u].copy(), csc_val[:u].copy()
+
+
 def from_coo(m, n, rows, cols, vals, te_rows, te_cols, te_vals):
     csr_ptr, csr_idx, csr_val, csc_ptr, csc_idx, csc_val = compress(m, n, rows, cols, vals)
     return RatingMatrix(m, n, csr_ptr, csr_idx, csr_val, csc_ptr, csc_idx, csc_val,

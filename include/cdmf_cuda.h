@@ -200,6 +200,43 @@ int cdmf_cuda_stats(const cdmf_handle* h, cdmf_stats* s);
 int cdmf_cuda_get_bincfg(const cdmf_handle* h, cdmf_bincfg* c);
 int cdmf_cuda_set_bincfg(cdmf_handle* h, const cdmf_bincfg* c);
 int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms);
+/* Canonical CSR and CSC of a COO rating list, built on the GPU: the arrays
+ * the reference's data/a/a_compress.py:130-155 writes with scipy's
+ * tocsr()/tocsc() and src/tools.cpp:271-347 loads.  Entries are sorted by
+ * (row, column); duplicate (row, column) pairs are summed in FP64 in input
+ * order and stored as float; the CSC lists rows ascending inside each column.
+ * All arrays are host memory.  csr_idx, csr_val, csc_idx and csc_val must hold
+ * nnz entries; *nnz_out receives the number of distinct entries (<= nnz).
+ * An index outside [0, m) x [0, n) returns CDMF_ERR_INVALID. */
+int cdmf_cuda_compress(int64_t m, int64_t n, int64_t nnz, const uint32_t* rows, const uint32_t* cols,
+                       const double* vals, int device, uint32_t* csr_ptr, uint32_t* csr_idx, float* csr_val,
+                       uint32_t* csc_ptr, uint32_t* csc_idx, float* csc_val, int64_t* nnz_out);
+/* Dual SpMV handle for callers of the reference's CSR5 library
+ * (anonymouslibHandle, src/anonymouslib_opencl.h:11-26, as driven by
+ * src/cdmf_csr5.cpp:205-286).  All matrix and vector arrays are the caller's
+ * device memory and must stay alive while the handle uses them.
+ *   cdmf_spmv_create(m, n)                 anonymouslibHandle(m, n) + device
+ *   cdmf_spmv_input_csr(nnz, ptr, idx, val)  inputCSR (row pointers checked)
+ *   cdmf_spmv_as_csr5 / cdmf_spmv_as_csr    asCSR5 (plans the load-balanced
+ *                                          work, checks column indices) / asCSR
+ *   cdmf_spmv_set_x(x)                     setX
+ *   cdmf_spmv_run(alpha, y_t, y_b, ms)     spmv: y_t[i] = sum_j val_ij x[col_j],
+ *                                          y_b[i] = sum_j x[col_j]^2; alpha is not
+ *                                          applied, as in the reference kernel
+ *                                          (csr5_spmv.cl:135-147); returns
+ *                                          CDMF_ERR_UNSUPPORTED in CSR form, as the
+ *                                          reference returns ANONYMOUSLIB_UNSUPPORTED_CSR_SPMV.
+ * Sums run in a fixed order: repeated calls give identical bits. */
+typedef struct cdmf_spmv cdmf_spmv;
+int cdmf_spmv_create(int64_t m, int64_t n, int device, cdmf_spmv** out);
+void cdmf_spmv_destroy(cdmf_spmv* s);
+const char* cdmf_spmv_last_error(const cdmf_spmv* s);
+int cdmf_spmv_input_csr(cdmf_spmv* s, int64_t nnz, const uint32_t* row_ptr, const uint32_t* col_idx,
+                        const float* val);
+int cdmf_spmv_as_csr5(cdmf_spmv* s);
+int cdmf_spmv_as_csr(cdmf_spmv* s);
+int cdmf_spmv_set_x(cdmf_spmv* s, const float* x);
+int cdmf_spmv_run(cdmf_spmv* s, float alpha, float* y_t, float* y_b, double* ms);
 /* Page-locked host memory for inputs and outputs of cdmf_cuda_train /
  * create / get_factors (copies from it run at full link speed).  NULL on
  * failure. */

@@ -81,3 +81,23 @@ def test_null_arguments():
     assert lib.cdmf_cuda_run(None, 1, None) == -1
     assert lib.cdmf_cuda_get_factors(None, None, None) == -1
     lib.cdmf_cuda_destroy(None)
+
+
+def test_anonymouslib_header_compiles_and_links(tmp_path):
+    """The C++ face of the dual SpMV handle: a caller written against the
+    reference's anonymouslibHandle calls compiles and links against the library."""
+    import subprocess
+    from cdmf_gb300 import _build
+    src = tmp_path / "use.cpp"
+    src.write_text(
+        "#include <cdmf_anonymouslib.hpp>\n"
+        "int main() {\n"
+        "  cdmf::anonymouslibHandle<int, unsigned int, float> A(4, 5);\n"
+        "  double t = 0; A.setSigma(4); (void)A.asCSR5_(&t);\n"
+        "  return A.lastError() == nullptr;\n"
+        "}\n")
+    out = tmp_path / "use"
+    r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(out),
+                        "-L", os.path.dirname(_build.LIB), "-lcdmf_cuda", "-Wl,-rpath," + os.path.dirname(_build.LIB)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
