@@ -48,7 +48,7 @@ def test_versions_and_modes_run(tmp_path, flags):
     its = [float(b) for _, b in ITER.findall(out)]
     assert len(its) == 5
     # flags reach the engine: 16-bit residual storage moves the RMSE of this
-    # 26-rating toy problem by about 1e-3 (the mixed-precision accuracy bar
+    # 5 x 5, 9-rating toy problem by about 1e-3 (the mixed-precision accuracy bar
     # itself is tested at realistic size in test_parity_gpu.py)
     tol = 5e-3 if "bf16" in flags else 5e-5
     assert abs(its[-1] - z["rmse"][-1]) <= tol, (its, z["rmse"])
