@@ -19,6 +19,8 @@
 // device scratch is allocated per call and freed before it returns.
 #include <cdmf_cuda.h>
 
+#include "gpu_build.h"
+
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 
@@ -232,3 +234,175 @@ extern "C" int cdmf_cuda_compress(int64_t m, int64_t n, int64_t nnz, const uint3
     *nnz_out = U;
     return CDMF_OK;
 }
+
+// ============================================================================
+// Degree relabelling on the GPU (the engine's create step for the line
+// layout).  Same result as relabel() in relabel.cpp, bit for bit:
+//   rows / columns ordered by decreasing degree, ties by id (stable radix
+//   sort of the complemented degree over ids in order);
+//   new CSR: entries keyed (new row, new column), stable-sorted;
+//   new CSC: stable sort of the new CSR entries by column.
+// ============================================================================
+
+namespace {
+
+__global__ void row_degrees(const uint32_t* __restrict__ ptr, int64_t m, uint32_t* __restrict__ key,
+                            uint32_t* __restrict__ id) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        key[i] = ~(ptr[i + 1] - ptr[i]);   // ascending key = descending degree
+        id[i] = (uint32_t)i;
+    }
+}
+
+__global__ void count_cols(const uint32_t* __restrict__ idx, int64_t nnz, uint32_t* __restrict__ cnt) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(cnt + idx[q], 1u);
+}
+
+__global__ void col_keys(const uint32_t* __restrict__ cnt, int64_t n, uint32_t* __restrict__ key,
+                         uint32_t* __restrict__ id) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        key[j] = ~cnt[j];
+        id[j] = (uint32_t)j;
+    }
+}
+
+__global__ void invert(const uint32_t* __restrict__ old_of_new, int64_t len, uint32_t* __restrict__ new_of_old) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < len; q += (int64_t)gridDim.x * blockDim.x)
+        new_of_old[old_of_new[q]] = (uint32_t)q;
+}
+
+// new row q: its length, for the scan that gives the new row pointers
+__global__ void new_lengths(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ row_old, int64_t m,
+                            uint32_t* __restrict__ len) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < m; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = row_old[q];
+        len[q] = ptr[i + 1] - ptr[i];
+    }
+}
+
+// one warp per caller row: key (new row, new column) and the caller position
+__global__ void entry_keys(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ idx,
+                           const uint32_t* __restrict__ row_new, const uint32_t* __restrict__ col_new, int64_t m,
+                           uint64_t n, uint64_t* __restrict__ key, uint32_t* __restrict__ pos) {
+    const int64_t warps = (int64_t)gridDim.x * blockDim.x / 32;
+    const int lane = threadIdx.x & 31;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; i < m; i += warps) {
+        const uint64_t q = row_new[i];
+        for (uint32_t s = ptr[i] + lane; s < ptr[i + 1]; s += 32) {
+            key[s] = q * n + col_new[idx[s]];
+            pos[s] = s;
+        }
+    }
+}
+
+__global__ void csr_fill(const uint64_t* __restrict__ key, const uint32_t* __restrict__ pos,
+                         const float* __restrict__ uval, int64_t nnz, uint64_t n, uint32_t* __restrict__ idx,
+                         float* __restrict__ val, uint32_t* __restrict__ iota) {
+    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < nnz; o += (int64_t)gridDim.x * blockDim.x) {
+        idx[o] = (uint32_t)(key[o] % n);
+        val[o] = uval[pos[o]];
+        iota[o] = (uint32_t)o;
+    }
+}
+
+__global__ void csc_fill(const uint32_t* __restrict__ from_csr, const uint64_t* __restrict__ key,
+                         const float* __restrict__ val, int64_t nnz, uint64_t n, uint32_t* __restrict__ cidx,
+                         float* __restrict__ cval, uint32_t* __restrict__ to_csc) {
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nnz; v += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t o = from_csr[v];
+        cidx[v] = (uint32_t)(key[o] / n);
+        cval[v] = val[o];
+        if (to_csc) to_csc[o] = (uint32_t)v;
+    }
+}
+
+}  // namespace
+
+namespace cdmf {
+
+int gpu_relabel(const cdmf_problem& p, cudaStream_t s, GpuRelabel& out, std::vector<void*>& allocs) {
+    const int64_t m = p.m, n = p.n, N = p.nnz;
+    auto keep = [&](auto** ptr, size_t count) -> bool {
+        using T = std::remove_pointer_t<std::remove_reference_t<decltype(*ptr)>>;
+        if (cudaMalloc((void**)ptr, std::max<size_t>(1, count) * sizeof(T)) != cudaSuccess) return false;
+        allocs.push_back((void*)*ptr);
+        return true;
+    };
+    if (!keep(&out.uptr, m + 1) || !keep(&out.uidx, N) || !keep(&out.csr_ptr, m + 1) || !keep(&out.csr_idx, N) || !keep(&out.csr_val, N) || !keep(&out.csc_ptr, n + 1) ||
+        !keep(&out.csc_idx, N) || !keep(&out.csc_val, N) || !keep(&out.csr_pos, N) || !keep(&out.csc_from_csr, N) ||
+        !keep(&out.to_csc, N))
+        return CDMF_ERR_ALLOC;
+    Scratch S;
+    uint32_t *uptr = out.uptr, *uidx = out.uidx, *rkey, *rkey2, *rid, *ccnt, *ckey, *ckey2, *cid, *row_old, *col_old, *row_new, *col_new,
+        *nlen, *pos_a, *iota, *col_sorted;
+    uint64_t *key_a, *key_b;
+    float* uval;
+    if (!S.get(&uval, N) || !S.get(&rkey, m) || !S.get(&rkey2, m) ||
+        !S.get(&rid, m) || !S.get(&ccnt, n) || !S.get(&ckey, n) || !S.get(&ckey2, n) || !S.get(&cid, n) ||
+        !S.get(&row_old, m) || !S.get(&col_old, n) || !S.get(&row_new, m) || !S.get(&col_new, n) ||
+        !S.get(&nlen, m + 1) || !S.get(&pos_a, N) || !S.get(&iota, N) || !S.get(&col_sorted, N) || !S.get(&key_a, N) ||
+        !S.get(&key_b, N))
+        return CDMF_ERR_ALLOC;
+#define RC(x) do { if ((x) != cudaSuccess) return CDMF_ERR_CUDA; } while (0)
+    RC(cudaMemcpyAsync(uptr, p.csr_row_ptr, 4 * (size_t)(m + 1), cudaMemcpyHostToDevice, s));
+    RC(cudaMemcpyAsync(uidx, p.csr_col_idx, 4 * (size_t)N, cudaMemcpyHostToDevice, s));
+    RC(cudaMemcpyAsync(uval, p.csr_val, 4 * (size_t)N, cudaMemcpyHostToDevice, s));
+    RC(cudaMemsetAsync(ccnt, 0, 4 * (size_t)n, s));
+    // degree orders
+    row_degrees<<<grid_for(m), kThreads, 0, s>>>(uptr, m, rkey, rid);
+    count_cols<<<grid_for(N), kThreads, 0, s>>>(uidx, N, ccnt);
+    col_keys<<<grid_for(n), kThreads, 0, s>>>(ccnt, n, ckey, cid);
+    RC(cudaGetLastError());
+    const int kbits = bits_for((uint64_t)m * (uint64_t)n - 1), cbits = bits_for((uint64_t)n - 1);
+    size_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0;
+    RC(cub::DeviceRadixSort::SortPairs(nullptr, t0, rkey, rkey2, rid, row_old, m, 0, 32, s));
+    RC(cub::DeviceRadixSort::SortPairs(nullptr, t1, ckey, ckey2, cid, col_old, n, 0, 32, s));
+    RC(cub::DeviceScan::ExclusiveSum(nullptr, t2, nlen, out.csr_ptr, m + 1, s));
+    RC(cub::DeviceRadixSort::SortPairs(nullptr, t3, key_a, key_b, pos_a, out.csr_pos, N, 0, kbits, s));
+    RC(cub::DeviceRadixSort::SortPairs(nullptr, t4, out.csr_idx, col_sorted, iota, out.csc_from_csr, N, 0, cbits, s));
+    const size_t tb = std::max({t0, t1, t2, t3, t4});
+    char* tmp = nullptr;
+    if (!S.get(&tmp, tb)) return CDMF_ERR_ALLOC;
+    size_t tbv = tb;
+    RC(cub::DeviceRadixSort::SortPairs(tmp, tbv, rkey, rkey2, rid, row_old, m, 0, 32, s));
+    tbv = tb;
+    RC(cub::DeviceRadixSort::SortPairs(tmp, tbv, ckey, ckey2, cid, col_old, n, 0, 32, s));
+    invert<<<grid_for(m), kThreads, 0, s>>>(row_old, m, row_new);
+    invert<<<grid_for(n), kThreads, 0, s>>>(col_old, n, col_new);
+    // new row pointers: lengths in the new order, scanned (the extra last
+    // element of nlen is 0, so ptr[m] = nnz)
+    RC(cudaMemsetAsync(nlen + m, 0, 4, s));
+    new_lengths<<<grid_for(m), kThreads, 0, s>>>(uptr, row_old, m, nlen);
+    RC(cudaGetLastError());
+    tbv = tb;
+    RC(cub::DeviceScan::ExclusiveSum(tmp, tbv, nlen, out.csr_ptr, m + 1, s));
+    // entries in (new row, new column) order
+    entry_keys<<<grid_for(32 * m), kThreads, 0, s>>>(uptr, uidx, row_new, col_new, m, (uint64_t)n, key_a, pos_a);
+    RC(cudaGetLastError());
+    tbv = tb;
+    RC(cub::DeviceRadixSort::SortPairs(tmp, tbv, key_a, key_b, pos_a, out.csr_pos, N, 0, kbits, s));
+    csr_fill<<<grid_for(N), kThreads, 0, s>>>(key_b, out.csr_pos, uval, N, (uint64_t)n, out.csr_idx, out.csr_val, iota);
+    RC(cudaGetLastError());
+    // CSC: stable transposition
+    tbv = tb;
+    RC(cub::DeviceRadixSort::SortPairs(tmp, tbv, out.csr_idx, col_sorted, iota, out.csc_from_csr, N, 0, cbits, s));
+    csc_fill<<<grid_for(N), kThreads, 0, s>>>(out.csc_from_csr, key_b, out.csr_val, N, (uint64_t)n, out.csc_idx,
+                                              out.csc_val, out.to_csc);
+    line_pointers<<<grid_for(N), kThreads, 0, s>>>(col_sorted, N, n, out.csc_ptr);
+    RC(cudaGetLastError());
+    // host copies of what the set-up plans with
+    out.row_old.resize(m);
+    out.col_old.resize(n);
+    out.hptr_r.resize(m + 1);
+    out.hptr_c.resize(n + 1);
+    RC(cudaMemcpyAsync(out.row_old.data(), row_old, 4 * (size_t)m, cudaMemcpyDeviceToHost, s));
+    RC(cudaMemcpyAsync(out.col_old.data(), col_old, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    RC(cudaMemcpyAsync(out.hptr_r.data(), out.csr_ptr, 4 * (size_t)(m + 1), cudaMemcpyDeviceToHost, s));
+    RC(cudaMemcpyAsync(out.hptr_c.data(), out.csc_ptr, 4 * (size_t)(n + 1), cudaMemcpyDeviceToHost, s));
+    RC(cudaStreamSynchronize(s));
+#undef RC
+    return CDMF_OK;
+}
+
+}  // namespace cdmf

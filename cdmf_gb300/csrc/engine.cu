@@ -21,6 +21,7 @@
 #include "sweep_kernels.cuh"
 #include "refresh_kernels.cuh"
 #include "objective_kernels.cuh"
+#include "gpu_build.h"
 #include "tile_kernels.cuh"
 #include "blocked_kernels.cuh"
 #include "relabel.h"
@@ -170,6 +171,9 @@ struct cdmf_handle {
     bool relabeled = false;
     uvec<uint32_t> row_old, col_old, csr_pos, csc_pos, csc_from_csr;
     uvec<uint32_t> ucsr_ptr, ucsr_idx;   // caller's CSR structure, for csc_pos on demand
+    // relabelling built on the device: the position maps and the caller's CSR
+    // structure stay there until a state move needs them on the host
+    uint32_t *d_csr_pos = nullptr, *d_csc_from_csr = nullptr, *d_ucsr_ptr = nullptr, *d_ucsr_idx = nullptr;
     // host copies of the line pointers (engine numbering) and the bin plan
     std::vector<uint32_t> hptr_r, hptr_c;
     BinCfg cfg;
@@ -797,8 +801,24 @@ void scatter_ids(const float* eng, float* user, uint32_t k, int64_t len, const u
     }
 }
 
+int need_host_maps(cdmf_handle* h) {
+    if (!h->d_csr_pos || !h->csr_pos.empty()) return CDMF_OK;
+    const int64_t N = h->nnz;
+    h->csr_pos.resize(N);
+    h->csc_from_csr.resize(N);
+    h->ucsr_ptr.resize(h->m + 1);
+    h->ucsr_idx.resize(N);
+    CU(h, cudaMemcpyAsync(h->csr_pos.data(), h->d_csr_pos, 4 * (size_t)N, cudaMemcpyDeviceToHost, h->s));
+    CU(h, cudaMemcpyAsync(h->csc_from_csr.data(), h->d_csc_from_csr, 4 * (size_t)N, cudaMemcpyDeviceToHost, h->s));
+    CU(h, cudaMemcpyAsync(h->ucsr_ptr.data(), h->d_ucsr_ptr, 4 * (size_t)(h->m + 1), cudaMemcpyDeviceToHost, h->s));
+    CU(h, cudaMemcpyAsync(h->ucsr_idx.data(), h->d_ucsr_idx, 4 * (size_t)N, cudaMemcpyDeviceToHost, h->s));
+    CU(h, cudaStreamSynchronize(h->s));
+    return CDMF_OK;
+}
+
 int need_csc_pos(cdmf_handle* h) {
     if (!h->relabeled || !h->csc_pos.empty() || h->nnz == 0) return CDMF_OK;
+    if (int r = need_host_maps(h)) return r;
     if (!relabel_csc_positions(h->m, h->n, h->ucsr_ptr.data(), h->ucsr_idx.data(), h->csr_pos, h->csc_from_csr,
                                h->csc_pos))
         return fail(h, CDMF_ERR_ALLOC, "caller CSC positions");
@@ -1014,7 +1034,11 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     Relabel RL;
     const cdmf_problem q0 = *p;
     cdmf_problem q = *p;
-    if (o->relabel && !seq_order && p->nnz > 0) {
+    // relabel 1 with the line layout: the renumbered structures are built on
+    // the device below; otherwise (relabel 2, or the blocked layout, which
+    // plans on host copies) on the host here
+    const bool relabel_on_gpu = o->relabel == 1 && !seq_order && p->nnz > 0 && o->layout != CDMF_LAYOUT_BLOCKED;
+    if (o->relabel && !seq_order && p->nnz > 0 && !relabel_on_gpu) {
         if (!relabel(*p, RL)) return CDMF_ERR_INVALID;
         q.csr_row_ptr = RL.csr_ptr.data();
         q.csr_col_idx = RL.csr_idx.data();
@@ -1051,9 +1075,45 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if (cudaEventCreate(&h->ev_start) != cudaSuccess || cudaEventCreate(&h->ev_stop) != cudaSuccess)
         return bail(CDMF_ERR_CUDA);
     const int64_t m = p->m, n = p->n, N = p->nnz, k = o->k;
-    if ((r = dalloc(h, &h->csr_ptr, m + 1)) || (r = dalloc(h, &h->csr_idx, N)) || (r = dalloc(h, &h->csc_ptr, n + 1)) ||
-        (r = dalloc(h, &h->csc_idx, N)) || (r = dalloc(h, &h->csr_val, N)) || (r = dalloc(h, &h->csc_val, N)) ||
-        (r = dalloc(h, (char**)&h->res_csr, N * h->rbytes)) || (r = dalloc(h, (char**)&h->res_csc, N * h->rbytes)) ||
+    GpuRelabel G;
+    uvec<uint32_t> te_row, te_col;
+    if (relabel_on_gpu) {
+        if ((r = gpu_relabel(*p, h->s, G, h->allocs)))
+            return bail(r == CDMF_ERR_ALLOC ? r : fail(h, r, "degree relabelling on the device"));
+        h->relabeled = true;
+        h->row_old = std::move(G.row_old);
+        h->col_old = std::move(G.col_old);
+        h->csr_ptr = G.csr_ptr;
+        h->csr_idx = G.csr_idx;
+        h->csr_val = G.csr_val;
+        h->csc_ptr = G.csc_ptr;
+        h->csc_idx = G.csc_idx;
+        h->csc_val = G.csc_val;
+        h->d_csr_pos = G.csr_pos;
+        h->d_csc_from_csr = G.csc_from_csr;
+        h->d_ucsr_ptr = G.uptr;
+        h->d_ucsr_idx = G.uidx;
+        // the test set in the new numbering
+        uvec<uint32_t> row_new(m), col_new(n);
+        for (int64_t q = 0; q < m; ++q) row_new[h->row_old[q]] = (uint32_t)q;
+        for (int64_t q = 0; q < n; ++q) col_new[h->col_old[q]] = (uint32_t)q;
+        te_row.resize(p->nnz_test);
+        te_col.resize(p->nnz_test);
+#pragma omp parallel for schedule(static)
+        for (int64_t e = 0; e < p->nnz_test; ++e) {
+            te_row[e] = row_new[p->test_row[e]];
+            te_col[e] = col_new[p->test_col[e]];
+        }
+        q.test_row = te_row.data();
+        q.test_col = te_col.data();
+        p = &q;
+        phase("relabel (GPU)");
+    } else if ((r = dalloc(h, &h->csr_ptr, m + 1)) || (r = dalloc(h, &h->csr_idx, N)) ||
+               (r = dalloc(h, &h->csc_ptr, n + 1)) || (r = dalloc(h, &h->csc_idx, N)) ||
+               (r = dalloc(h, &h->csr_val, N)) || (r = dalloc(h, &h->csc_val, N))) {
+        return bail(r);
+    }
+    if ((r = dalloc(h, (char**)&h->res_csr, N * h->rbytes)) || (r = dalloc(h, (char**)&h->res_csc, N * h->rbytes)) ||
         (r = dalloc(h, &h->W, k * m)) || (r = dalloc(h, &h->H, k * n)) || (r = dalloc(h, &h->P, m)) ||
         (r = dalloc(h, &h->Q, n)) ||
         (r = dalloc(h, &h->te_row, h->nt)) || (r = dalloc(h, &h->te_col, h->nt)) || (r = dalloc(h, &h->te_val, h->nt)))
@@ -1069,10 +1129,12 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         if (e != cudaSuccess) return fail(h, CDMF_ERR_CUDA, cudaGetErrorString(e));
         return CDMF_OK;
     };
-    if ((r = up(h->csr_ptr, p->csr_row_ptr, 4 * (m + 1))) || (r = up(h->csr_idx, p->csr_col_idx, 4 * N)) ||
-        (r = up(h->csc_ptr, p->csc_col_ptr, 4 * (n + 1))) || (r = up(h->csc_idx, p->csc_row_idx, 4 * N)) ||
-        (r = up(h->csr_val, p->csr_val, 4 * N)) || (r = up(h->csc_val, p->csc_val, 4 * N)) ||
-        (r = up(h->te_row, p->test_row, 4 * h->nt)) || (r = up(h->te_col, p->test_col, 4 * h->nt)) ||
+    if (!relabel_on_gpu &&
+        ((r = up(h->csr_ptr, p->csr_row_ptr, 4 * (m + 1))) || (r = up(h->csr_idx, p->csr_col_idx, 4 * N)) ||
+         (r = up(h->csc_ptr, p->csc_col_ptr, 4 * (n + 1))) || (r = up(h->csc_idx, p->csc_row_idx, 4 * N)) ||
+         (r = up(h->csr_val, p->csr_val, 4 * N)) || (r = up(h->csc_val, p->csc_val, 4 * N))))
+        return bail(r);
+    if ((r = up(h->te_row, p->test_row, 4 * h->nt)) || (r = up(h->te_col, p->test_col, 4 * h->nt)) ||
         (r = up(h->te_val, p->test_val, 4 * h->nt)))
         return bail(r);
     if (cudaMemsetAsync(h->rmse_count, 0, 4, h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
@@ -1091,8 +1153,10 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if (h->rt != 0) {
         // CSR position -> CSC position; also proves the CSC arrays are the
         // transpose of the CSR arrays, which the refresh scatter relies on
-        uvec<uint32_t> to_csc(N);
-        if (h->relabeled) {
+        uvec<uint32_t> to_csc(relabel_on_gpu ? 0 : N);
+        if (relabel_on_gpu) {
+            // built on the device with the copies
+        } else if (h->relabeled) {
             // both copies were built from the CSR: invert the CSC -> CSR map
 #pragma omp parallel for schedule(static)
             for (int64_t o = 0; o < N; ++o) to_csc[h->csc_from_csr[o]] = (uint32_t)o;
@@ -1111,7 +1175,8 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         h->kp = (o->k + 3) / 4 * 4;
         const int64_t nchunks = (N + kRefreshChunk - 1) / kRefreshChunk;
         h->ref_grid = (int)std::max<int64_t>(1, std::min<int64_t>(152 * 8, nchunks));
-        if ((r = dalloc(h, &h->to_csc, N)) || (r = dalloc(h, &h->Wrm, (size_t)m * h->kp)) ||
+        if (relabel_on_gpu) h->to_csc = G.to_csc;
+        if ((!relabel_on_gpu && (r = dalloc(h, &h->to_csc, N))) || (r = dalloc(h, &h->Wrm, (size_t)m * h->kp)) ||
             (r = dalloc(h, &h->Hrm, (size_t)n * h->kp)) || (r = dalloc(h, &h->ref_part, h->ref_grid)) ||
             (r = dalloc(h, &h->drift_out, 1)) || (r = dalloc(h, &h->ref_count, 1)) || (r = dalloc(h, &h->nonfinite, 1)))
             return bail(r);
@@ -1121,7 +1186,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
             for (int64_t q = 0; q < N; ++q) to_csc[q] = h->hmap_c[to_csc[q]];
             h->ref_to_csr = h->bcsr.map;
         }
-        if ((r = up(h->to_csc, to_csc.data(), 4 * N))) return bail(r);
+        if (!relabel_on_gpu && (r = up(h->to_csc, to_csc.data(), 4 * N))) return bail(r);
         phase("refresh map");
         if (cudaMemsetAsync(h->ref_count, 0, 4, h->s) != cudaSuccess ||
             cudaMemsetAsync(h->nonfinite, 0, 8, h->s) != cudaSuccess ||
@@ -1130,15 +1195,20 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
             return bail(CDMF_ERR_CUDA);
     }
     h->seq = seq;
-    h->hptr_r.assign(p->csr_row_ptr, p->csr_row_ptr + m + 1);
-    h->hptr_c.assign(p->csc_col_ptr, p->csc_col_ptr + n + 1);
-    if ((r = upload_bins(h, h->csr, plan_bins(p->csr_row_ptr, m, seq, h->cfg))) ||
-        (r = upload_bins(h, h->csc, plan_bins(p->csc_col_ptr, n, seq, h->cfg))))
+    if (relabel_on_gpu) {
+        h->hptr_r = std::move(G.hptr_r);
+        h->hptr_c = std::move(G.hptr_c);
+    } else {
+        h->hptr_r.assign(p->csr_row_ptr, p->csr_row_ptr + m + 1);
+        h->hptr_c.assign(p->csc_col_ptr, p->csc_col_ptr + n + 1);
+    }
+    if ((r = upload_bins(h, h->csr, plan_bins(h->hptr_r.data(), m, seq, h->cfg))) ||
+        (r = upload_bins(h, h->csc, plan_bins(h->hptr_c.data(), n, seq, h->cfg))))
         return bail(r);
     phase("bins");
     h->tiles = o->version == 3 && !seq && !h->blocked;
-    if (h->tiles && ((r = upload_tiles(h, h->tcsr, p->csr_row_ptr, m, N)) ||
-                     (r = upload_tiles(h, h->tcsc, p->csc_col_ptr, n, N))))
+    if (h->tiles && ((r = upload_tiles(h, h->tcsr, h->hptr_r.data(), m, N)) ||
+                     (r = upload_tiles(h, h->tcsc, h->hptr_c.data(), n, N))))
         return bail(r);
     // fresh state: W := 0 until set, H := 0, residual := ratings
     if (cudaMemsetAsync(h->W, 0, sizeof(float) * k * m, h->s) != cudaSuccess ||

@@ -57,7 +57,8 @@ def make_opts(k, lambda_, maxiter=5, maxinneriter=5, version=1, residual="f32", 
     o.rmse_each_outer = int(bool(rmse_each_outer))
     o.use_graph = int(bool(use_graph))
     o.device, o.threads_per_block, o.verbose = int(device), int(threads_per_block), int(verbose)
-    o.relabel = int(bool(relabel))
+    # True / 1: relabel (on the GPU for the line layout); "host" / 2: relabel on the host
+    o.relabel = 2 if relabel == "host" else int(relabel) if not isinstance(relabel, bool) else int(relabel)
     o.autotune = int(bool(autotune))
     if layout is not None:
         o.layout = {"lines": 0, "blocked": 1}[layout] if isinstance(layout, str) else int(layout)

@@ -88,7 +88,9 @@ typedef struct {
     int32_t device;           /* CUDA device ordinal */
     int32_t verbose;
     int32_t relabel;          /* 1: renumber rows and columns by degree inside the engine
-                                 (tree order only; results come back in the caller's numbering) */
+                                 (tree order only; results come back in the caller's numbering),
+                                 built on the GPU for the line layout; 2: the same numbering
+                                 built on the host */
     int32_t autotune;         /* 1: pick the bin thresholds by timing candidates on this matrix
                                  at create (cached per matrix shape in the process) */
     int32_t layout;           /* CDMF_LAYOUT_*: how the residual copies are stored (tree order) */

@@ -424,3 +424,21 @@ def test_blocked_deterministic_and_state_roundtrip(cpu_scale):
             outs.append(e.state())
     for f in ("W", "H", "res_csc", "res_csr"):
         assert np.array_equal(bits(outs[0][f]), bits(outs[1][f])), f
+
+
+@pytest.mark.parametrize("residual", ["f32", "bf16"])
+def test_device_relabel_matches_host_relabel(cpu_scale, residual):
+    """The degree relabelling built on the GPU at create gives the same engine
+    as the host build: identical factors, residual state and RMSE, bit for bit."""
+    R, run, W0, ref = cpu_scale
+    out = []
+    for where in (True, "host"):
+        with engine.Engine(R, run["k"], run["lambda_"], 3, 1, residual=residual, relabel=where) as e:
+            e.set_factors(W0)
+            rm = e.run(2)
+            st = e.state()
+            out.append((rm, st))
+    (rm1, s1), (rm2, s2) = out
+    assert np.array_equal(rm1, rm2)
+    for key in ("W", "H", "res_csc", "res_csr"):
+        assert np.array_equal(bits(s1[key]), bits(s2[key])), key
