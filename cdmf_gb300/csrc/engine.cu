@@ -37,6 +37,7 @@
 #include <tuple>
 #include <cstdio>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -174,6 +175,10 @@ struct cdmf_handle {
     // relabelling built on the device: the position maps and the caller's CSR
     // structure stay there until a state move needs them on the host
     uint32_t *d_csr_pos = nullptr, *d_csc_from_csr = nullptr, *d_ucsr_ptr = nullptr, *d_ucsr_idx = nullptr;
+    // narrow matrices: CSR sweeps gather from a shared-memory copy of Q
+    bool smemq = false;
+    int sms = 0;
+    uint32_t* smemq_queue = nullptr;
     // host copies of the line pointers (engine numbering) and the bin plan
     std::vector<uint32_t> hptr_r, hptr_c;
     BinCfg cfg;
@@ -522,7 +527,62 @@ int launch_blocked(cdmf_handle* h, int kind, const SweepArgs& A, int mode, bool 
     return CDMF_OK;
 }
 
+template <int RT>
+void smemq_attrs(int bytes) {
+    cudaFuncSetAttribute(sweep_smemq_kernel<RT, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(sweep_smemq_kernel<RT, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(sweep_smemq_kernel<RT, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(sweep_smemq_kernel<RT, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+// Whether the CSR sweeps of this matrix can stage Q in shared memory; sets
+// the kernels' dynamic shared memory limit once per process and device.
+bool smemq_possible(int device, int64_t n, int* sms) {
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return false;
+    const int64_t need = 12 * n + 1024;   // three float planes + the static shared memory of the teams
+    if (n <= 0 || need > optin) return false;
+    static std::mutex mu;
+    static std::set<int> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.insert(device).second) {
+        smemq_attrs<0>(optin - 1024);
+        smemq_attrs<1>(optin - 1024);
+        smemq_attrs<2>(optin - 1024);
+    }
+    return true;
+}
+
+template <int RT>
+void smemq_rt(const SweepArgs& A, bool sub, bool add, unsigned grid, size_t smem, uint32_t nb, uint32_t* queue,
+              cudaStream_t s) {
+    if (sub && add) sweep_smemq_kernel<RT, true, true><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
+    else if (sub) sweep_smemq_kernel<RT, true, false><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
+    else if (add) sweep_smemq_kernel<RT, false, true><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
+    else sweep_smemq_kernel<RT, false, false><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
+}
+
 int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A, int mode, bool sub, bool add) {
+    if (mode == M_CSR && h->smemq && !h->blocked && !h->tiles) {
+        const uint32_t nb = D.nx + D.nc + D.nwb + D.ngb + D.ntb;
+        if (nb == 0) return CDMF_OK;
+        const size_t smem = 12 * (size_t)A.ncross;
+        {
+            Timed tm(h, kind);
+            CU(h, cudaMemsetAsync(h->smemq_queue, 0, 4, h->s));
+            switch (h->rt) {
+                case 0: smemq_rt<0>(A, sub, add, (unsigned)h->sms, smem, nb, h->smemq_queue, h->s); break;
+                case 1: smemq_rt<1>(A, sub, add, (unsigned)h->sms, smem, nb, h->smemq_queue, h->s); break;
+                default: smemq_rt<2>(A, sub, add, (unsigned)h->sms, smem, nb, h->smemq_queue, h->s); break;
+            }
+        }
+        CU(h, cudaGetLastError());
+        h->st.launches++;
+        h->st.sweep_csr_launches++;
+        return CDMF_OK;
+    }
     if (h->blocked) return launch_blocked(h, kind, A, mode, sub, add);
     if (h->tiles) {
         const DevTiles& D3 = kind == K_CSC ? h->tcsc : h->tcsr;
@@ -597,6 +657,7 @@ void feature_args(cdmf_handle* h, uint32_t t, int it, SweepArgs& A, SweepArgs& B
     B.out = Wt;
     if (first) {
         B.Q = h->Q;
+        B.ncross = (uint32_t)n;
         B.b = Wp;
         B.d = Wt;
     } else {
@@ -1210,6 +1271,10 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if (h->tiles && ((r = upload_tiles(h, h->tcsr, h->hptr_r.data(), m, N)) ||
                      (r = upload_tiles(h, h->tcsc, h->hptr_c.data(), n, N))))
         return bail(r);
+    if (!h->blocked && !h->tiles && N > 0 && smemq_possible(o->device, n, &h->sms) && !std::getenv("CDMF_NO_SMEMQ")) {
+        if ((r = dalloc(h, &h->smemq_queue, 1))) return bail(r);
+        h->smemq = true;
+    }
     // fresh state: W := 0 until set, H := 0, residual := ratings
     if (cudaMemsetAsync(h->W, 0, sizeof(float) * k * m, h->s) != cudaSuccess ||
         cudaMemsetAsync(h->H, 0, sizeof(float) * k * n, h->s) != cudaSuccess)

@@ -63,6 +63,7 @@ constexpr int M_PLAIN = 0;  // inner iterations >= 2: y only, no residual writes
 constexpr int M_CSC = 1;    // first CSC sweep of a feature: P gathers, emits Q
 constexpr int M_CSR = 2;    // first CSR sweep of a feature: Q gathers
 constexpr int M_DUAL = 3;   // dual SpMV (CSR5-style front end): y gathers, raw sums out
+constexpr int M_CSRS = 4;   // M_CSR with the cross table staged in shared memory (narrow matrices)
 
 struct XTask {            // one chunk of a split line
     uint32_t line, beg, end, slot;
@@ -95,6 +96,44 @@ struct SweepArgs {
     float2* part;                  // split-line partials
     uint32_t* xcount;              // split-line arrival counters (left at 0)
     float* out2;                   // M_DUAL: sum of y^2 per line (out gets the sum of y * r)
+    uint32_t ncross;               // M_CSRS: entries of the cross table (columns)
+};
+
+// The cross table of an M_CSRS sweep, as three float planes (a | c | y) in
+// dynamic shared memory.
+extern __shared__ float cdmf_qsm[];
+
+// Thread teams that run the work of one sweep block.
+// CtaTeam: the whole CTA (kBlock threads).
+struct CtaTeam {
+    static __device__ __forceinline__ uint32_t tid() { return threadIdx.x; }
+    static __device__ __forceinline__ void sync() { __syncthreads(); }
+    static __device__ __forceinline__ float2* red() {
+        __shared__ float2 sm[kWarps];
+        return sm;
+    }
+    static __device__ __forceinline__ int* flag() {
+        __shared__ int f;
+        return &f;
+    }
+};
+// SubTeam: one of kSubs groups of kBlock threads in a kSubs * kBlock CTA,
+// synchronised by its own named barrier (ids 1..kSubs).
+constexpr int kSubs = 4;
+struct SubTeam {
+    static __device__ __forceinline__ uint32_t sub() { return threadIdx.x / kBlock; }
+    static __device__ __forceinline__ uint32_t tid() { return threadIdx.x % kBlock; }
+    static __device__ __forceinline__ void sync() {
+        asm volatile("bar.sync %0, %1;" ::"r"(sub() + 1), "r"(kBlock) : "memory");
+    }
+    static __device__ __forceinline__ float2* red() {
+        __shared__ float2 sm[kSubs][kWarps];
+        return sm[sub()];
+    }
+    static __device__ __forceinline__ int* flag() {
+        __shared__ int f[kSubs];
+        return &f[sub()];
+    }
 };
 
 // ---- streaming loads -----------------------------------------------------------
@@ -216,6 +255,10 @@ __device__ __forceinline__ void fetch(const SweepArgs& A, uint32_t i, float& a, 
         a = q.x;
         c = q.y;
         y = q.z;
+    } else if (MODE == M_CSRS) {
+        a = cdmf_qsm[i];
+        c = cdmf_qsm[A.ncross + i];
+        y = cdmf_qsm[2 * A.ncross + i];
     } else {
         a = c = 0.0f;
         y = __ldg(A.y + i);
@@ -356,13 +399,14 @@ __device__ __forceinline__ void warp_sum2(float& g, float& h) {
 
 // CTA-wide sum; the result is valid in thread 0.  Fixed shape: per-warp xor
 // tree, then warps 0..7 in order.
+template <class Team = CtaTeam>
 __device__ __forceinline__ void cta_sum2(float& g, float& h) {
-    __shared__ float2 sm[kWarps];
+    float2* sm = Team::red();
     warp_sum2(g, h);
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) sm[w] = make_float2(g, h);
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    const uint32_t w = Team::tid() >> 5;
+    if ((Team::tid() & 31) == 0) sm[w] = make_float2(g, h);
+    Team::sync();
+    if (Team::tid() == 0) {
         float G = sm[0].x, Hs = sm[0].y;
         for (int q = 1; q < kWarps; ++q) { G = __fadd_rn(G, sm[q].x); Hs = __fadd_rn(Hs, sm[q].y); }
         g = G;
@@ -400,24 +444,25 @@ __device__ __forceinline__ void line_scalars(const SweepArgs& A, uint32_t j, flo
 }
 
 // Work of block b of one sweep (b in [0, nx + nc + nwb + ngb + ntb)).
-template <int RT, int MODE, bool SUB, bool ADD>
+template <int RT, int MODE, bool SUB, bool ADD, class Team = CtaTeam>
 __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
+    const uint32_t tid = Team::tid();
     if (b < A.nx) {                                        // split-line chunk
         const XTask T = A.xt[b];
         float bj, dj;
         line_scalars<MODE, SUB, ADD>(A, T.line, bj, dj);
         float g = 0.0f, h = 0.0f;
-        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, T.beg, T.end, threadIdx.x, bj, dj, g, h);
-        cta_sum2(g, h);
-        __shared__ int last;
-        if (threadIdx.x == 0) {
+        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, T.beg, T.end, tid, bj, dj, g, h);
+        cta_sum2<Team>(g, h);
+        int& last = *Team::flag();
+        if (tid == 0) {
             A.part[T.slot] = make_float2(g, h);
             __threadfence();
             const uint32_t prev = atomicAdd(A.xcount + T.xl, 1u);
             last = (prev == T.nchunks - 1);
         }
-        __syncthreads();
-        if (last && threadIdx.x == 0) {
+        Team::sync();
+        if (last && tid == 0) {
             __threadfence();
             float G = 0.0f, Hs = 0.0f;
             for (uint32_t q = 0; q < T.nchunks; ++q) {
@@ -438,16 +483,16 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
         float bj, dj;
         line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
         float g = 0.0f, h = 0.0f;
-        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, beg, end, threadIdx.x, bj, dj, g, h);
-        cta_sum2(g, h);
-        if (threadIdx.x == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
+        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, beg, end, tid, bj, dj, g, h);
+        cta_sum2<Team>(g, h);
+        if (tid == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
         return;
     }
     b -= A.nc;
     if (b < A.nwb) {                                       // one line per warp
-        const uint32_t w = b * kWarps + (threadIdx.x >> 5);
+        const uint32_t w = b * kWarps + (tid >> 5);
         if (w >= A.nw) return;
-        const uint32_t lane = threadIdx.x & 31;
+        const uint32_t lane = tid & 31;
         const uint32_t j = A.wl[w];
         const uint32_t beg = A.ptr[j], end = A.ptr[j + 1];
         float bj, dj;
@@ -460,8 +505,8 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
     }
     b -= A.nwb;
     if (b < A.ngb) {                                       // one line per 8-lane group
-        const uint32_t slot = b * (kBlock / 8) + (threadIdx.x >> 3);
-        const uint32_t sub = threadIdx.x & 7;
+        const uint32_t slot = b * (kBlock / 8) + (tid >> 3);
+        const uint32_t sub = tid & 7;
         const bool valid = slot < A.ng;
         const uint32_t j = valid ? A.gl[slot] : 0u;
         const uint32_t beg = valid ? A.ptr[j] : 0u, end = valid ? A.ptr[j + 1] : 0u;
@@ -474,7 +519,7 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
         return;
     }
     b -= A.ngb;
-    const uint32_t t = b * kBlock + threadIdx.x;           // one line per thread
+    const uint32_t t = b * kBlock + tid;           // one line per thread
     if (t >= A.nt) return;
     const uint32_t j = A.tl[t];
     const uint32_t beg = A.ptr[j], end = A.ptr[j + 1];
@@ -501,6 +546,34 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
 template <int RT, int MODE, bool SUB, bool ADD>
 __global__ void CDMF_SWEEP_BOUNDS sweep_kernel(const SweepArgs A) {
     sweep_block<RT, MODE, SUB, ADD>(A, blockIdx.x);
+}
+
+// CSR sweep of a narrow matrix (the cross table fits in shared memory): one
+// CTA of kSubs * kBlock threads per SM copies Q into shared memory as three
+// float planes, then its kSubs teams pull sweep blocks from a device work
+// queue and run them with every gather served from shared memory.  The
+// arithmetic is M_CSR's, element for element.
+template <int RT, bool SUB, bool ADD>
+__global__ void __launch_bounds__(kBlock * kSubs, 1) sweep_smemq_kernel(const SweepArgs A, uint32_t nblocks,
+                                                                      uint32_t* queue) {
+    const uint32_t n = A.ncross;
+    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+        const float4 v = __ldg(A.Q + j);
+        cdmf_qsm[j] = v.x;
+        cdmf_qsm[n + j] = v.y;
+        cdmf_qsm[2 * n + j] = v.z;
+    }
+    __syncthreads();
+    __shared__ uint32_t blk[kSubs];
+    const uint32_t sub = SubTeam::sub();
+    for (;;) {
+        if (SubTeam::tid() == 0) blk[sub] = atomicAdd(queue, 1u);
+        SubTeam::sync();
+        const uint32_t b = blk[sub];
+        SubTeam::sync();
+        if (b >= nblocks) return;
+        sweep_block<RT, M_CSRS, SUB, ADD, SubTeam>(A, b);
+    }
 }
 
 // Many problems' sweeps in one persistent launch: resident blocks pull block

@@ -442,3 +442,23 @@ def test_device_relabel_matches_host_relabel(cpu_scale, residual):
     assert np.array_equal(rm1, rm2)
     for key in ("W", "H", "res_csc", "res_csr"):
         assert np.array_equal(bits(s1[key]), bits(s2[key])), key
+
+
+@pytest.mark.parametrize("residual", ["f32", "bf16"])
+def test_shared_memory_cross_table_matches_global(cpu_scale, residual, monkeypatch):
+    """Narrow matrices stage the CSR sweep's cross table in shared memory; the
+    result must equal the L1/L2 gather path bit for bit (CDMF_NO_SMEMQ turns
+    the staging off at create)."""
+    R, run, W0, ref = cpu_scale
+    out = []
+    for off in (False, True):
+        if off:
+            monkeypatch.setenv("CDMF_NO_SMEMQ", "1")
+        with engine.Engine(R, run["k"], run["lambda_"], 3, 1, residual=residual) as e:
+            e.set_factors(W0)
+            rm = e.run(3)
+            out.append((rm, e.state()))
+    (rm1, s1), (rm2, s2) = out
+    assert np.array_equal(rm1, rm2)
+    for key in ("W", "H", "res_csc", "res_csr"):
+        assert np.array_equal(bits(s1[key]), bits(s2[key])), key
