@@ -1271,7 +1271,11 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if (h->tiles && ((r = upload_tiles(h, h->tcsr, h->hptr_r.data(), m, N)) ||
                      (r = upload_tiles(h, h->tcsc, h->hptr_c.data(), n, N))))
         return bail(r);
-    if (!h->blocked && !h->tiles && N > 0 && smemq_possible(o->device, n, &h->sms) && !std::getenv("CDMF_NO_SMEMQ")) {
+    // measured on the Netflix-shaped matrix: FP32 CSR sweeps +6 % with the
+    // shared-memory table, 16-bit ones -6 % (the 1024-thread CTAs hold 32
+    // warps per SM against 48 for the global path), so FP32 only
+    if (h->rt == 0 && !h->blocked && !h->tiles && N > 0 && smemq_possible(o->device, n, &h->sms) &&
+        !std::getenv("CDMF_NO_SMEMQ")) {
         if ((r = dalloc(h, &h->smemq_queue, 1))) return bail(r);
         h->smemq = true;
     }
