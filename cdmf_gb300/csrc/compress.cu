@@ -329,18 +329,18 @@ int gpu_relabel(const cdmf_problem& p, cudaStream_t s, GpuRelabel& out, std::vec
         allocs.push_back((void*)*ptr);
         return true;
     };
-    if (!keep(&out.uptr, m + 1) || !keep(&out.uidx, N) || !keep(&out.csr_ptr, m + 1) || !keep(&out.csr_idx, N) || !keep(&out.csr_val, N) || !keep(&out.csc_ptr, n + 1) ||
+    if (!keep(&out.d_row_old, m) || !keep(&out.d_col_old, n) || !keep(&out.uptr, m + 1) || !keep(&out.uidx, N) || !keep(&out.csr_ptr, m + 1) || !keep(&out.csr_idx, N) || !keep(&out.csr_val, N) || !keep(&out.csc_ptr, n + 1) ||
         !keep(&out.csc_idx, N) || !keep(&out.csc_val, N) || !keep(&out.csr_pos, N) || !keep(&out.csc_from_csr, N) ||
         !keep(&out.to_csc, N))
         return CDMF_ERR_ALLOC;
     Scratch S;
-    uint32_t *uptr = out.uptr, *uidx = out.uidx, *rkey, *rkey2, *rid, *ccnt, *ckey, *ckey2, *cid, *row_old, *col_old, *row_new, *col_new,
-        *nlen, *pos_a, *iota, *col_sorted;
+    uint32_t *uptr = out.uptr, *uidx = out.uidx, *row_old = out.d_row_old, *col_old = out.d_col_old;
+    uint32_t *rkey, *rkey2, *rid, *ccnt, *ckey, *ckey2, *cid, *row_new, *col_new, *nlen, *pos_a, *iota, *col_sorted;
     uint64_t *key_a, *key_b;
     float* uval;
     if (!S.get(&uval, N) || !S.get(&rkey, m) || !S.get(&rkey2, m) ||
         !S.get(&rid, m) || !S.get(&ccnt, n) || !S.get(&ckey, n) || !S.get(&ckey2, n) || !S.get(&cid, n) ||
-        !S.get(&row_old, m) || !S.get(&col_old, n) || !S.get(&row_new, m) || !S.get(&col_new, n) ||
+        !S.get(&row_new, m) || !S.get(&col_new, n) ||
         !S.get(&nlen, m + 1) || !S.get(&pos_a, N) || !S.get(&iota, N) || !S.get(&col_sorted, N) || !S.get(&key_a, N) ||
         !S.get(&key_b, N))
         return CDMF_ERR_ALLOC;

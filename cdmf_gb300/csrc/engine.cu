@@ -175,6 +175,9 @@ struct cdmf_handle {
     // relabelling built on the device: the position maps and the caller's CSR
     // structure stay there until a state move needs them on the host
     uint32_t *d_csr_pos = nullptr, *d_csc_from_csr = nullptr, *d_ucsr_ptr = nullptr, *d_ucsr_idx = nullptr;
+    // relabelled factors cross the boundary through a device permutation
+    uint32_t *d_row_old = nullptr, *d_col_old = nullptr;
+    float* ftmp = nullptr;           // k * max(m, n) staging for the caller's factor order
     // narrow matrices: CSR sweeps gather from a shared-memory copy of Q
     bool smemq = false;
     int sms = 0;
@@ -812,6 +815,36 @@ int refresh_residual(cdmf_handle* h) {
     return CDMF_OK;
 }
 
+// Factor rows between the caller's numbering and the engine's: gather
+// (dst[t][q] = src[t][old[q]]) on the way in, scatter on the way out.
+__global__ void permute_factors_kernel(const float* __restrict__ src, float* __restrict__ dst,
+                                       const uint32_t* __restrict__ old_of_new, uint32_t k, int64_t len, int scatter) {
+    const int64_t total = (int64_t)k * len;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = e / len, q = e - t * len;
+        const int64_t o = t * len + old_of_new[q];
+        if (scatter) dst[o] = src[e];
+        else dst[e] = src[o];
+    }
+}
+
+// Caller-order factors (host) -> engine order (device), through ftmp.
+int factors_in(cdmf_handle* h, const float* user, float* dev, int64_t len, const uint32_t* old_of_new) {
+    const size_t bytes = sizeof(float) * h->o.k * len;
+    CU(h, cudaMemcpyAsync(h->ftmp, user, bytes, cudaMemcpyHostToDevice, h->s));
+    permute_factors_kernel<<<1216, kBlock, 0, h->s>>>(h->ftmp, dev, old_of_new, h->o.k, len, 0);
+    CU(h, cudaGetLastError());
+    return CDMF_OK;
+}
+
+int factors_out(cdmf_handle* h, const float* dev, float* user, int64_t len, const uint32_t* old_of_new) {
+    const size_t bytes = sizeof(float) * h->o.k * len;
+    permute_factors_kernel<<<1216, kBlock, 0, h->s>>>(dev, h->ftmp, old_of_new, h->o.k, len, 1);
+    CU(h, cudaGetLastError());
+    CU(h, cudaMemcpyAsync(user, h->ftmp, bytes, cudaMemcpyDeviceToHost, h->s));
+    return CDMF_OK;
+}
+
 __global__ void f32_to_res_kernel(const float* __restrict__ src, void* __restrict__ dst, int64_t count, int rt) {
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
         if (rt == 1) ((__nv_bfloat16*)dst)[q] = __float2bfloat16_rn(src[q]);
@@ -852,13 +885,6 @@ void gather_ids(const float* user, float* eng, uint32_t k, int64_t len, const uv
         const float* u = user + (size_t)t * len;
         float* e = eng + (size_t)t * len;
         for (int64_t q = 0; q < len; ++q) e[q] = u[old_of_new[q]];
-    }
-}
-void scatter_ids(const float* eng, float* user, uint32_t k, int64_t len, const uvec<uint32_t>& old_of_new) {
-    for (uint32_t t = 0; t < k; ++t) {
-        const float* e = eng + (size_t)t * len;
-        float* u = user + (size_t)t * len;
-        for (int64_t q = 0; q < len; ++q) u[old_of_new[q]] = e[q];
     }
 }
 
@@ -1154,6 +1180,8 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         h->d_csc_from_csr = G.csc_from_csr;
         h->d_ucsr_ptr = G.uptr;
         h->d_ucsr_idx = G.uidx;
+        h->d_row_old = G.d_row_old;
+        h->d_col_old = G.d_col_old;
         // the test set in the new numbering
         uvec<uint32_t> row_new(m), col_new(n);
         for (int64_t q = 0; q < m; ++q) row_new[h->row_old[q]] = (uint32_t)q;
@@ -1173,6 +1201,17 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
                (r = dalloc(h, &h->csc_ptr, n + 1)) || (r = dalloc(h, &h->csc_idx, N)) ||
                (r = dalloc(h, &h->csr_val, N)) || (r = dalloc(h, &h->csc_val, N))) {
         return bail(r);
+    }
+    if (h->relabeled) {
+        if ((r = dalloc(h, &h->ftmp, (size_t)k * std::max(m, n)))) return bail(r);
+        if (!relabel_on_gpu) {   // host-built numbering: its maps to the device
+            if ((r = dalloc(h, &h->d_row_old, m)) || (r = dalloc(h, &h->d_col_old, n))) return bail(r);
+            if (cudaMemcpyAsync(h->d_row_old, h->row_old.data(), 4 * (size_t)m, cudaMemcpyHostToDevice, h->s) !=
+                    cudaSuccess ||
+                cudaMemcpyAsync(h->d_col_old, h->col_old.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, h->s) !=
+                    cudaSuccess)
+                return bail(CDMF_ERR_CUDA);
+        }
     }
     if ((r = dalloc(h, (char**)&h->res_csr, N * h->rbytes)) || (r = dalloc(h, (char**)&h->res_csc, N * h->rbytes)) ||
         (r = dalloc(h, &h->W, k * m)) || (r = dalloc(h, &h->H, k * n)) || (r = dalloc(h, &h->P, m)) ||
@@ -1300,22 +1339,21 @@ int cdmf_cuda_set_factors(cdmf_handle* h, const float* W0, const float* H0) {
     if (!h) return CDMF_ERR_INVALID;
     CU(h, cudaSetDevice(h->o.device));
     const size_t wb = sizeof(float) * h->o.k * h->m, hb = sizeof(float) * h->o.k * h->n;
-    std::vector<float> tw, th;
+    int r;
     if (h->relabeled && W0) {
-        tw.resize((size_t)h->o.k * h->m);
-        gather_ids(W0, tw.data(), h->o.k, h->m, h->row_old);
-        W0 = tw.data();
+        if ((r = factors_in(h, W0, h->W, h->m, h->d_row_old))) return r;
+    } else if (W0) {
+        CU(h, cudaMemcpyAsync(h->W, W0, wb, cudaMemcpyHostToDevice, h->s));
+    } else {
+        CU(h, cudaMemsetAsync(h->W, 0, wb, h->s));
     }
     if (h->relabeled && H0) {
-        th.resize((size_t)h->o.k * h->n);
-        gather_ids(H0, th.data(), h->o.k, h->n, h->col_old);
-        H0 = th.data();
+        if ((r = factors_in(h, H0, h->H, h->n, h->d_col_old))) return r;
+    } else if (H0) {
+        CU(h, cudaMemcpyAsync(h->H, H0, hb, cudaMemcpyHostToDevice, h->s));
+    } else {
+        CU(h, cudaMemsetAsync(h->H, 0, hb, h->s));
     }
-    if (W0) CU(h, cudaMemcpyAsync(h->W, W0, wb, cudaMemcpyHostToDevice, h->s));
-    else CU(h, cudaMemsetAsync(h->W, 0, wb, h->s));
-    if (H0) CU(h, cudaMemcpyAsync(h->H, H0, hb, cudaMemcpyHostToDevice, h->s));
-    else CU(h, cudaMemsetAsync(h->H, 0, hb, h->s));
-    int r;
     if ((r = reset_residual(h, h->res_csr, h->csr_val)) || (r = reset_residual(h, h->res_csc, h->csc_val))) return r;
     h->pending = -1;
     h->p_for = -1;
@@ -1389,16 +1427,18 @@ int cdmf_cuda_run(cdmf_handle* h, int n_outer, double* rmse_out) {
 int cdmf_cuda_get_factors(cdmf_handle* h, float* W, float* H) {
     if (!h) return CDMF_ERR_INVALID;
     CU(h, cudaSetDevice(h->o.device));
-    std::vector<float> tw, th;
-    float* wd = W;
-    float* hd = H;
-    if (h->relabeled && W) { tw.resize((size_t)h->o.k * h->m); wd = tw.data(); }
-    if (h->relabeled && H) { th.resize((size_t)h->o.k * h->n); hd = th.data(); }
-    if (W) CU(h, cudaMemcpyAsync(wd, h->W, sizeof(float) * h->o.k * h->m, cudaMemcpyDeviceToHost, h->s));
-    if (H) CU(h, cudaMemcpyAsync(hd, h->H, sizeof(float) * h->o.k * h->n, cudaMemcpyDeviceToHost, h->s));
+    int r;
+    if (h->relabeled && W) {
+        if ((r = factors_out(h, h->W, W, h->m, h->d_row_old))) return r;
+    } else if (W) {
+        CU(h, cudaMemcpyAsync(W, h->W, sizeof(float) * h->o.k * h->m, cudaMemcpyDeviceToHost, h->s));
+    }
+    if (h->relabeled && H) {
+        if ((r = factors_out(h, h->H, H, h->n, h->d_col_old))) return r;
+    } else if (H) {
+        CU(h, cudaMemcpyAsync(H, h->H, sizeof(float) * h->o.k * h->n, cudaMemcpyDeviceToHost, h->s));
+    }
     CU(h, cudaStreamSynchronize(h->s));
-    if (h->relabeled && W) scatter_ids(wd, W, h->o.k, h->m, h->row_old);
-    if (h->relabeled && H) scatter_ids(hd, H, h->o.k, h->n, h->col_old);
     return CDMF_OK;
 }
 
@@ -1713,10 +1753,21 @@ int cdmf_cuda_rmse_coo(uint32_t k, int64_t m, int64_t n, const float* W, const f
 int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* H, double* rmse_out, cdmf_outer_cb cb,
                     void* user) {
     if (!p || !o || !W || !H) return CDMF_ERR_INVALID;
+    // o->verbose: phase times on stderr
+    auto t_last = std::chrono::steady_clock::now();
+    auto phase = [&](const char* what) {
+        if (!o->verbose) return;
+        const auto t = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[cdmf] train: %-12s %8.1f ms\n", what,
+                     std::chrono::duration<double, std::milli>(t - t_last).count());
+        t_last = t;
+    };
     cdmf_handle* h = nullptr;
     int r = cdmf_cuda_create(p, o, &h);
     if (r) return r;
+    phase("create");
     if ((r = cdmf_cuda_set_factors(h, W, nullptr))) { cdmf_cuda_destroy(h); return r; }
+    phase("set_factors");
     const bool want_rmse = o->rmse_each_outer && p->nnz_test > 0;
     double total_ms = 0;
     for (int it = 0; it < o->maxiter; ++it) {
@@ -1727,8 +1778,11 @@ int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* 
         if (cb) cb(it + 1, want_rmse ? rm : -1.0, total_ms, user);
     }
     h->st.train_ms = total_ms;
+    phase("outer loop");
     r = cdmf_cuda_get_factors(h, W, H);
+    phase("get_factors");
     cdmf_cuda_destroy(h);
+    phase("destroy");
     return r;
 }
 

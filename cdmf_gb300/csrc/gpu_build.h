@@ -22,6 +22,7 @@ struct GpuRelabel {
     uint32_t* csc_from_csr = nullptr;   // new CSC position -> new CSR position
     uint32_t* to_csc = nullptr;         // new CSR position -> new CSC position
     uint32_t *uptr = nullptr, *uidx = nullptr;   // the caller's CSR structure (device copy)
+    uint32_t *d_row_old = nullptr, *d_col_old = nullptr;   // new id -> caller id (device)
     uvec<uint32_t> row_old, col_old;    // new id -> caller id (host)
     std::vector<uint32_t> hptr_r, hptr_c;   // new row / column pointers (host)
 };

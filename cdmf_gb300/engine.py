@@ -177,13 +177,23 @@ class Engine:
         return list(c), list(z)
 
 
-def train(R, W, k, lambda_, maxiter, maxinneriter, **kw):
-    """One-shot engine call (cdmf_cuda_train): returns (W, H, rmse per outer)."""
+def train(R, W, k, lambda_, maxiter, maxinneriter, H=None, inplace=False, **kw):
+    """One-shot engine call (cdmf_cuda_train): returns (W, H, rmse per outer).
+
+    inplace=True trains the caller's W (float32, C-contiguous) in place and
+    writes H into the caller's array (float32, k x n): with page-locked arrays
+    (_lib.pinned_empty) the copies run at full link speed."""
     lib = _lib.load()
     o = make_opts(k, lambda_, maxiter, maxinneriter, **kw)
     p = _problem(R)
-    W = np.ascontiguousarray(W, np.float32).copy()
-    H = np.zeros((k, R.n), np.float32)
+    if inplace:
+        if W.dtype != np.float32 or not W.flags["C_CONTIGUOUS"] or W.shape != (k, R.m):
+            raise ValueError("inplace W must be a C-contiguous float32 array of shape (k, m)")
+        if H is None or H.dtype != np.float32 or not H.flags["C_CONTIGUOUS"] or H.shape != (k, R.n):
+            raise ValueError("inplace needs H: a C-contiguous float32 array of shape (k, n)")
+    else:
+        W = np.ascontiguousarray(W, np.float32).copy()
+        H = np.zeros((k, R.n), np.float32)
     rm = np.zeros(max(1, maxiter), np.float64)
     check(lib.cdmf_cuda_train(ctypes.byref(p), ctypes.byref(o), ptr(W, ctypes.c_float), ptr(H, ctypes.c_float),
                               ptr(rm, ctypes.c_double), _lib.OUTER_CB(), None), "cdmf_cuda_train")
