@@ -284,6 +284,9 @@ def main():
     e2e = None
     if not args.quick:
         e2e = run_e2e(R, W0, k, lam, T, args, dist, ws, device)
+    fmt = None
+    if not args.quick and rank == 0:
+        fmt = measure_formats(R, peak)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         v, f, s = cpu_sample(R, run, W0, threads, args.cpu_budget)
@@ -327,6 +330,8 @@ def main():
         line["mixed_vs_fp32"] = value / comp["value"] if args.compare == "f32" else None
     line["refresh_ms_per_outer"] = head["refresh_ms_per_outer"]
     line["create_s"] = head["create_s"]
+    if fmt is not None:
+        line["formats"] = fmt
     line["rmse_ms_per_outer"] = head["rmse_ms_per_outer"]
     print(json.dumps(line), flush=True)
 
@@ -370,6 +375,49 @@ def bench_batch(args, threads):
         "gpu_launches": st["launches"], "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
+
+
+def measure_formats(R, peak):
+    """The format-build and dual-SpMV entry points on the same matrix:
+    cdmf_cuda_compress from the shuffled host COO (upload, sorts, download
+    included) and one cdmf_spmv_run over the CSR (kernel time; compulsory
+    bytes = index, value and row pointers, x once, 8 B written per row)."""
+    import ctypes
+    import torch
+    from cdmf_gb300 import formats, _lib
+    rows, cols, vals = R.coo()
+    perm = np.random.default_rng(0).permutation(rows.size)
+    rows, cols, vals = rows[perm], cols[perm], vals[perm].astype(np.float64)
+    formats.compress_gpu(R.m, R.n, rows[:1000], cols[:1000], vals[:1000])   # warm-up
+    t0 = time.perf_counter()
+    got = formats.compress_gpu(R.m, R.n, rows, cols, vals)
+    compress_s = time.perf_counter() - t0
+    same = all(np.array_equal(a.view(np.uint32), b.view(np.uint32)) for a, b in
+               zip(got, (R.csr_ptr, R.csr_idx, R.csr_val, R.csc_ptr, R.csc_idx, R.csc_val)))
+    lib = _lib.load()
+    dev = lambda a: torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).cuda()
+    dp, di, dv = dev(R.csr_ptr), dev(R.csr_idx), dev(R.csr_val)
+    dx = torch.rand(R.n, dtype=torch.float32, device="cuda")
+    yt = torch.empty(R.m, dtype=torch.float32, device="cuda")
+    yb = torch.empty(R.m, dtype=torch.float32, device="cuda")
+    h = ctypes.c_void_p()
+    _lib.check(lib.cdmf_spmv_create(R.m, R.n, 0, ctypes.byref(h)), "cdmf_spmv_create")
+    try:
+        _lib.check(lib.cdmf_spmv_input_csr(h, R.nnz, dp.data_ptr(), di.data_ptr(), dv.data_ptr()), "input_csr")
+        _lib.check(lib.cdmf_spmv_as_csr5(h), "as_csr5")
+        _lib.check(lib.cdmf_spmv_set_x(h, dx.data_ptr()), "set_x")
+        ms = ctypes.c_double()
+        times = []
+        for _ in range(6):
+            _lib.check(lib.cdmf_spmv_run(h, 1.0, yt.data_ptr(), yb.data_ptr(), ctypes.byref(ms)), "spmv")
+            times.append(ms.value)
+    finally:
+        lib.cdmf_spmv_destroy(h)
+    spmv_ms = statistics.median(times[1:])
+    spmv_bytes = 8.0 * R.nnz + 4.0 * (R.m + 1) + 4.0 * R.n + 8.0 * R.m   # compulsory: x read once
+    return {"compress_s": compress_s, "compress_nnz": int(rows.size), "compress_matches_host_build": bool(same),
+            "spmv_ms": spmv_ms, "spmv_gbs": spmv_bytes / spmv_ms / 1e6,
+            "spmv_frac": spmv_bytes / spmv_ms / 1e6 / peak}
 
 
 def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
