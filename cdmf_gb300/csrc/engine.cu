@@ -1802,7 +1802,7 @@ int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* 
 
 namespace {
 
-enum { OP_PACK, OP_REFRESH, OP_GSWEEP, OP_FINISH, OP_RMSE };
+enum { OP_PACK, OP_REFRESH, OP_GSWEEP, OP_FINISH, OP_RMSE, OP_GREFRESH, OP_GRMSE };
 
 struct BatchOp {
     int kind;
@@ -1813,6 +1813,17 @@ struct BatchOp {
     int side;         // K_CSC / K_CSR
     uint32_t desc_off, nq, prefix_off, queue;
     int slot;         // RMSE slot
+    // GREFRESH / GRMSE: grid sizes; GREFRESH's transposes (second descriptor list)
+    uint32_t blocks = 0, desc2_off = 0, nq2 = 0, prefix2_off = 0, blocks2 = 0;
+};
+
+// Descriptor lists of the grouped (all-problem) launches of one batched run.
+struct BatchPlan {
+    std::vector<SweepArgs> descs;
+    std::vector<uint32_t> prefix;
+    std::vector<RefreshDesc> rdescs;
+    std::vector<TransposeDesc> tdescs;
+    std::vector<RmseDesc> mdescs;
 };
 
 template <int RT>
@@ -1856,6 +1867,12 @@ struct cdmf_batch {
     size_t prefix_cap = 0;
     uint32_t* d_queue = nullptr;
     size_t queue_cap = 0;
+    RefreshDesc *d_rdesc = nullptr, *h_rdesc = nullptr;
+    size_t rdesc_cap = 0;
+    TransposeDesc *d_tdesc = nullptr, *h_tdesc = nullptr;
+    size_t tdesc_cap = 0;
+    RmseDesc *d_mdesc = nullptr, *h_mdesc = nullptr;
+    size_t mdesc_cap = 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int g_outer = -1;
@@ -1882,8 +1899,9 @@ int bfail(cdmf_batch* b, int code, const std::string& msg) {
 
 // Host plan of n_outer lockstep outer iterations (state of the handles is
 // simulated and restored).
-void plan_batch(cdmf_batch* B, int n_outer, std::vector<BatchOp>& ops, std::vector<SweepArgs>& descs,
-                std::vector<uint32_t>& prefix) {
+void plan_batch(cdmf_batch* B, int n_outer, std::vector<BatchOp>& ops, BatchPlan& plan) {
+    std::vector<SweepArgs>& descs = plan.descs;
+    std::vector<uint32_t>& prefix = plan.prefix;
     const int P = (int)B->hs.size();
     struct Saved { int pending, p_for, next; };
     std::vector<Saved> saved(P);
@@ -1891,11 +1909,56 @@ void plan_batch(cdmf_batch* B, int n_outer, std::vector<BatchOp>& ops, std::vect
     uint32_t queues = 0;
     for (int o = 0; o < n_outer; ++o) {
         const int oiter = B->hs[0]->next_oiter;
-        for (int q = 0; q < P; ++q) {
-            cdmf_handle* h = B->hs[q];
-            if (h->rt != 0 && oiter > 1 && h->nnz > 0) {
-                ops.push_back({OP_REFRESH, q, 0, 0, false, false, 0, 0, 0, 0, 0, 0});
+        {   // every problem's refresh (and its row-major factor copies) in two launches
+            BatchOp op{OP_GREFRESH, -1, 0, 0, false, false, 0, (uint32_t)plan.rdescs.size(), 0, 0, 0, 0};
+            op.desc2_off = (uint32_t)plan.tdescs.size();
+            std::vector<uint32_t> rp{0}, tp{0};
+            for (int q = 0; q < P; ++q) {
+                cdmf_handle* h = B->hs[q];
+                if (!(h->rt != 0 && oiter > 1 && h->nnz > 0)) continue;
+                const int tpend = h->pending;
+                const uint32_t kq = h->kp / 4;
+                RefreshDesc D;
+                D.ptr = h->csr_ptr;
+                D.idx = h->csr_idx;
+                D.val = h->csr_val;
+                D.to_csr = h->ref_to_csr;
+                D.to_csc = h->to_csc;
+                D.m = h->m;
+                D.nnz = h->nnz;
+                D.Wrm = h->Wrm;
+                D.Hrm = h->Hrm;
+                D.kp = h->kp;
+                D.slices = kq <= kRefG ? 1 : kq <= 2 * kRefG ? 2 : kq <= 4 * kRefG ? 4 : kq <= 8 * kRefG ? 8 : 0;
+                D.res_csr = h->res_csr;
+                D.res_csc = h->res_csc;
+                D.pa = tpend >= 0 ? h->H + (size_t)tpend * h->n : nullptr;
+                D.pb = tpend >= 0 ? h->W + (size_t)tpend * h->m : nullptr;
+                D.part = h->ref_part;
+                D.counter = h->ref_count;
+                D.drift_out = h->drift_out;
+                D.nonfinite = h->nonfinite;
+                plan.rdescs.push_back(D);
+                rp.push_back(rp.back() + (uint32_t)h->ref_grid);
+                const uint32_t ty = (h->kp + 31) / 32;
+                const TransposeDesc Tw{h->W, h->Wrm, h->o.k, h->kp, h->m, (uint32_t)((h->m + 31) / 32)};
+                const TransposeDesc Th{h->H, h->Hrm, h->o.k, h->kp, h->n, (uint32_t)((h->n + 31) / 32)};
+                plan.tdescs.push_back(Tw);
+                tp.push_back(tp.back() + Tw.tiles_x * ty);
+                plan.tdescs.push_back(Th);
+                tp.push_back(tp.back() + Th.tiles_x * ty);
                 h->pending = -1;
+            }
+            op.nq = (uint32_t)(plan.rdescs.size() - op.desc_off);
+            if (op.nq) {
+                op.nq2 = (uint32_t)(plan.tdescs.size() - op.desc2_off);
+                op.prefix_off = (uint32_t)prefix.size();
+                prefix.insert(prefix.end(), rp.begin(), rp.end());
+                op.blocks = rp.back();
+                op.prefix2_off = (uint32_t)prefix.size();
+                prefix.insert(prefix.end(), tp.begin(), tp.end());
+                op.blocks2 = tp.back();
+                ops.push_back(op);
             }
         }
         for (uint32_t t = 0; t < B->kmax && B->T > 0; ++t) {
@@ -1943,10 +2006,26 @@ void plan_batch(cdmf_batch* B, int n_outer, std::vector<BatchOp>& ops, std::vect
                 feature_finish(B->hs[q], t);
             }
         }
-        for (int q = 0; q < P; ++q) {
-            if (B->hs[q]->o.rmse_each_outer && B->hs[q]->nt > 0)
-                ops.push_back({OP_RMSE, q, 0, 0, false, false, 0, 0, 0, 0, 0, o});
-            B->hs[q]->next_oiter++;
+        {   // every problem's test RMSE in one launch
+            BatchOp op{OP_GRMSE, -1, 0, 0, false, false, 0, (uint32_t)plan.mdescs.size(), 0, 0, 0, o};
+            std::vector<uint32_t> mp{0};
+            for (int q = 0; q < P; ++q) {
+                cdmf_handle* h = B->hs[q];
+                if (h->o.rmse_each_outer && h->nt > 0) {
+                    RmseDesc D{h->te_row, h->te_col, h->te_val, h->nt, h->m, h->n, h->W, h->H, h->o.k,
+                               h->rmse_part, h->rmse_count, h->rmse_out + o};
+                    plan.mdescs.push_back(D);
+                    mp.push_back(mp.back() + (uint32_t)h->rmse_grid);
+                }
+                h->next_oiter++;
+            }
+            op.nq = (uint32_t)(plan.mdescs.size() - op.desc_off);
+            if (op.nq) {
+                op.prefix_off = (uint32_t)prefix.size();
+                prefix.insert(prefix.end(), mp.begin(), mp.end());
+                op.blocks = mp.back();
+                ops.push_back(op);
+            }
         }
     }
     for (int q = 0; q < P; ++q) {
@@ -1971,9 +2050,18 @@ int grow_pair(cdmf_batch* B, T** d, T** hpin, size_t& cap, size_t need) {
     return CDMF_OK;
 }
 
-int execute_batch(cdmf_batch* B, const std::vector<BatchOp>& ops, size_t ndesc, size_t nprefix, uint32_t nqueue) {
-    BCU(B, cudaMemcpyAsync(B->d_desc, B->h_desc, sizeof(SweepArgs) * ndesc, cudaMemcpyHostToDevice, B->s));
-    BCU(B, cudaMemcpyAsync(B->d_prefix, B->h_prefix, 4 * nprefix, cudaMemcpyHostToDevice, B->s));
+int execute_batch(cdmf_batch* B, const std::vector<BatchOp>& ops, const BatchPlan& plan, uint32_t nqueue) {
+    BCU(B, cudaMemcpyAsync(B->d_desc, B->h_desc, sizeof(SweepArgs) * plan.descs.size(), cudaMemcpyHostToDevice, B->s));
+    BCU(B, cudaMemcpyAsync(B->d_prefix, B->h_prefix, 4 * plan.prefix.size(), cudaMemcpyHostToDevice, B->s));
+    if (!plan.rdescs.empty()) {
+        BCU(B, cudaMemcpyAsync(B->d_rdesc, B->h_rdesc, sizeof(RefreshDesc) * plan.rdescs.size(), cudaMemcpyHostToDevice,
+                               B->s));
+        BCU(B, cudaMemcpyAsync(B->d_tdesc, B->h_tdesc, sizeof(TransposeDesc) * plan.tdescs.size(),
+                               cudaMemcpyHostToDevice, B->s));
+    }
+    if (!plan.mdescs.empty())
+        BCU(B, cudaMemcpyAsync(B->d_mdesc, B->h_mdesc, sizeof(RmseDesc) * plan.mdescs.size(), cudaMemcpyHostToDevice,
+                               B->s));
     BCU(B, cudaMemsetAsync(B->d_queue, 0, 4 * std::max<uint32_t>(1, nqueue), B->s));
     for (const BatchOp& op : ops) {
         int r = CDMF_OK;
@@ -1982,6 +2070,30 @@ int execute_batch(cdmf_batch* B, const std::vector<BatchOp>& ops, size_t ndesc, 
             case OP_REFRESH: r = refresh_residual(B->hs[op.q]); break;
             case OP_FINISH: feature_finish(B->hs[op.q], op.t); break;
             case OP_RMSE: r = launch_rmse(B->hs[op.q], B->hs[op.q]->rmse_out + op.slot); break;
+            case OP_GREFRESH: {
+                grouped_row_major_kernel<<<op.blocks2, kBlock, 0, B->s>>>(B->d_tdesc + op.desc2_off,
+                                                                          B->d_prefix + op.prefix2_off, op.nq2);
+                const RefreshDesc* d = B->d_rdesc + op.desc_off;
+                const uint32_t* pre = B->d_prefix + op.prefix_off;
+                if (B->rt == 1) grouped_refresh_kernel<1><<<op.blocks, kBlock, 0, B->s>>>(d, pre, op.nq);
+                else grouped_refresh_kernel<2><<<op.blocks, kBlock, 0, B->s>>>(d, pre, op.nq);
+                BCU(B, cudaGetLastError());
+                B->st.launches += 2;
+                B->st.refresh_launches++;
+                for (cdmf_handle* h : B->hs)   // as refresh_residual leaves each problem
+                    if (h->rt != 0 && h->nnz > 0) {
+                        h->pending = -1;
+                        h->refreshed = true;
+                    }
+                break;
+            }
+            case OP_GRMSE:
+                grouped_rmse_kernel<<<op.blocks, kBlock, 0, B->s>>>(B->d_mdesc + op.desc_off, B->d_prefix + op.prefix_off,
+                                                                    op.nq);
+                BCU(B, cudaGetLastError());
+                B->st.launches++;
+                B->st.rmse_launches++;
+                break;
             case OP_GSWEEP: {
                 const SweepArgs* d = B->d_desc + op.desc_off;
                 const uint32_t* pre = B->d_prefix + op.prefix_off;
@@ -2022,6 +2134,10 @@ void cdmf_cuda_batch_destroy(cdmf_batch* B) {
     if (B->d_prefix) cudaFree(B->d_prefix);
     if (B->h_prefix) cudaFreeHost(B->h_prefix);
     if (B->d_queue) cudaFree(B->d_queue);
+    for (void* p : {(void*)B->d_rdesc, (void*)B->d_tdesc, (void*)B->d_mdesc})
+        if (p) cudaFree(p);
+    for (void* p : {(void*)B->h_rdesc, (void*)B->h_tdesc, (void*)B->h_mdesc})
+        if (p) cudaFreeHost(p);
     if (B->e0) cudaEventDestroy(B->e0);
     if (B->e1) cudaEventDestroy(B->e1);
     if (B->s) cudaStreamDestroy(B->s);
@@ -2090,9 +2206,10 @@ int cdmf_cuda_batch_run(cdmf_batch* B, int n_outer, double* rmse_out) {
         h->refreshed = false;
     }
     std::vector<BatchOp> ops;
-    std::vector<SweepArgs> descs;
-    std::vector<uint32_t> prefix;
-    plan_batch(B, n_outer, ops, descs, prefix);
+    BatchPlan plan;
+    plan_batch(B, n_outer, ops, plan);
+    const std::vector<SweepArgs>& descs = plan.descs;
+    const std::vector<uint32_t>& prefix = plan.prefix;
     uint32_t nqueue = 0;
     for (const BatchOp& op : ops)
         if (op.kind == OP_GSWEEP) nqueue = std::max(nqueue, op.queue + 1);
@@ -2118,6 +2235,12 @@ int cdmf_cuda_batch_run(cdmf_batch* B, int n_outer, double* rmse_out) {
                 B->st.launches++;
                 if (op.side == K_CSC) B->st.sweep_csc_launches++;
                 else B->st.sweep_csr_launches++;
+            } else if (op.kind == OP_GREFRESH) {
+                B->st.launches += 2;
+                B->st.refresh_launches++;
+            } else if (op.kind == OP_GRMSE) {
+                B->st.launches++;
+                B->st.rmse_launches++;
             }
         B->st.launches += B->g_single.launches;
         B->st.rmse_launches += B->g_single.rmse_launches;
@@ -2136,12 +2259,19 @@ int cdmf_cuda_batch_run(cdmf_batch* B, int n_outer, double* rmse_out) {
         }
         if (!B->d_queue && cudaMalloc((void**)&B->d_queue, 4) != cudaSuccess)
             return bfail(B, CDMF_ERR_ALLOC, "batch queues");
+        if ((r = grow_pair(B, &B->d_rdesc, &B->h_rdesc, B->rdesc_cap, std::max<size_t>(1, plan.rdescs.size()))) ||
+            (r = grow_pair(B, &B->d_tdesc, &B->h_tdesc, B->tdesc_cap, std::max<size_t>(1, plan.tdescs.size()))) ||
+            (r = grow_pair(B, &B->d_mdesc, &B->h_mdesc, B->mdesc_cap, std::max<size_t>(1, plan.mdescs.size()))))
+            return r;
         std::copy(descs.begin(), descs.end(), B->h_desc);
         std::copy(prefix.begin(), prefix.end(), B->h_prefix);
+        std::copy(plan.rdescs.begin(), plan.rdescs.end(), B->h_rdesc);
+        std::copy(plan.tdescs.begin(), plan.tdescs.end(), B->h_tdesc);
+        std::copy(plan.mdescs.begin(), plan.mdescs.end(), B->h_mdesc);
         if (B->use_graph) {
             if (B->gexec) { cudaGraphExecDestroy(B->gexec); B->gexec = nullptr; }
             BCU(B, cudaStreamBeginCapture(B->s, cudaStreamCaptureModeThreadLocal));
-            r = execute_batch(B, ops, descs.size(), prefix.size(), nqueue);
+            r = execute_batch(B, ops, plan, nqueue);
             cudaGraph_t g = nullptr;
             const cudaError_t e = cudaStreamEndCapture(B->s, &g);
             if (r || e != cudaSuccess) {
@@ -2168,7 +2298,7 @@ int cdmf_cuda_batch_run(cdmf_batch* B, int n_outer, double* rmse_out) {
             }
             BCU(B, cudaGraphLaunch(B->gexec, B->s));
         } else {
-            if ((r = execute_batch(B, ops, descs.size(), prefix.size(), nqueue))) return r;
+            if ((r = execute_batch(B, ops, plan, nqueue))) return r;
             for (int q = 0; q < P; ++q) B->hs[q]->next_oiter += n_outer;
         }
     }

@@ -62,13 +62,14 @@ constexpr int kRefG = 4;
 #define CDMF_PRAGMA_(x) _Pragma(#x)
 #define CDMF_PRAGMA(x) CDMF_PRAGMA_(x)
 
+// Block `bid` of `nblk` blocks of one refresh.
 template <int RT, int S>
-__global__ void __launch_bounds__(kBlock) refresh_warp_kernel(
+__device__ __forceinline__ void refresh_body(
     const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ idx, const float* __restrict__ val,
     const uint32_t* __restrict__ to_csr, const uint32_t* __restrict__ to_csc, int64_t m, int64_t nnz,
     const float* __restrict__ Wrm, const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr,
     void* __restrict__ res_csc, const float* __restrict__ pa, const float* __restrict__ pb_, double* part,
-    uint32_t* counter, double* drift_out, unsigned long long* nonfinite_out) {
+    uint32_t* counter, double* drift_out, unsigned long long* nonfinite_out, uint32_t bid, uint32_t nblk) {
     __shared__ uint32_t srow[2];
     constexpr unsigned FULL = 0xffffffffu;
     constexpr int kPer = 32 / kRefG;   // nonzeros per round
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(kBlock) refresh_warp_kernel(
     double drift = 0.0;
     unsigned bad = 0;
     const int64_t nchunks = (nnz + kRefreshChunk - 1) / kRefreshChunk;
-    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    for (int64_t c = bid; c < nchunks; c += nblk) {
         const int64_t p0 = c * kRefreshChunk;
         const int64_t p1 = (p0 + kRefreshChunk < nnz) ? p0 + kRefreshChunk : nnz;
         if (threadIdx.x < 2) {
@@ -184,18 +185,96 @@ __global__ void __launch_bounds__(kBlock) refresh_warp_kernel(
         double s = sm[0];
         unsigned long long b = smb[0];
         for (int q = 1; q < kWarps; ++q) { s = __dadd_rn(s, sm[q]); b += smb[q]; }
-        part[blockIdx.x] = s;
+        part[bid] = s;
         if (b) atomicAdd(nonfinite_out, b);
         __threadfence();
-        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+        last = (atomicAdd(counter, 1u) == nblk - 1);
     }
     __syncthreads();
     if (last && threadIdx.x == 0) {
         __threadfence();
         double s = 0.0;
-        for (uint32_t q = 0; q < gridDim.x; ++q) s = __dadd_rn(s, __ldcg(part + q));
+        for (uint32_t q = 0; q < nblk; ++q) s = __dadd_rn(s, __ldcg(part + q));
         *drift_out = s;
         *counter = 0;
+    }
+}
+
+template <int RT, int S>
+__global__ void __launch_bounds__(kBlock) refresh_warp_kernel(
+    const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ idx, const float* __restrict__ val,
+    const uint32_t* __restrict__ to_csr, const uint32_t* __restrict__ to_csc, int64_t m, int64_t nnz,
+    const float* __restrict__ Wrm, const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr,
+    void* __restrict__ res_csc, const float* __restrict__ pa, const float* __restrict__ pb_, double* part,
+    uint32_t* counter, double* drift_out, unsigned long long* nonfinite_out) {
+    refresh_body<RT, S>(ptr, idx, val, to_csr, to_csc, m, nnz, Wrm, Hrm, kp, res_csr, res_csc, pa, pb_, part, counter,
+                        drift_out, nonfinite_out, blockIdx.x, gridDim.x);
+}
+
+// The refreshes of many problems (one residual type) in one launch, and the
+// row-major factor copies they read, also in one launch.
+struct RefreshDesc {
+    const uint32_t *ptr, *idx;
+    const float* val;
+    const uint32_t *to_csr, *to_csc;
+    int64_t m, nnz;
+    const float *Wrm, *Hrm;
+    uint32_t kp, slices;   // slices: the S of refresh_warp_kernel (0 = any k)
+    void *res_csr, *res_csc;
+    const float *pa, *pb;
+    double* part;
+    uint32_t* counter;
+    double* drift_out;
+    unsigned long long* nonfinite;
+};
+
+template <int RT>
+__global__ void __launch_bounds__(kBlock) grouped_refresh_kernel(const RefreshDesc* __restrict__ descs,
+                                                                 const uint32_t* __restrict__ prefix, uint32_t nprob) {
+    const uint32_t q = group_of(prefix, nprob, blockIdx.x);
+    const RefreshDesc D = descs[q];
+    const uint32_t b = blockIdx.x - prefix[q], nb = prefix[q + 1] - prefix[q];
+#define CDMF_REFRESH_CASE(SS)                                                                                     \
+    refresh_body<RT, SS>(D.ptr, D.idx, D.val, D.to_csr, D.to_csc, D.m, D.nnz, D.Wrm, D.Hrm, D.kp, D.res_csr,      \
+                         D.res_csc, D.pa, D.pb, D.part, D.counter, D.drift_out, D.nonfinite, b, nb)
+    switch (D.slices) {
+        case 1: CDMF_REFRESH_CASE(1); break;
+        case 2: CDMF_REFRESH_CASE(2); break;
+        case 4: CDMF_REFRESH_CASE(4); break;
+        case 8: CDMF_REFRESH_CASE(8); break;
+        default: CDMF_REFRESH_CASE(0); break;
+    }
+#undef CDMF_REFRESH_CASE
+}
+
+struct TransposeDesc {
+    const float* X;     // k x len, feature-major
+    float* Y;           // len x kp, row-major
+    uint32_t k, kp;
+    int64_t len;
+    uint32_t tiles_x;   // 32-row tiles
+};
+
+static __global__ void __launch_bounds__(kBlock) grouped_row_major_kernel(const TransposeDesc* __restrict__ descs,
+                                                                   const uint32_t* __restrict__ prefix,
+                                                                   uint32_t nprob) {
+    __shared__ float tile[32][33];
+    const uint32_t q = group_of(prefix, nprob, blockIdx.x);
+    const TransposeDesc D = descs[q];
+    const uint32_t b = blockIdx.x - prefix[q];
+    const int64_t i0 = (int64_t)(b % D.tiles_x) * 32;
+    const uint32_t t0 = (b / D.tiles_x) * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int r = ty; r < 32; r += 8) {
+        const uint32_t t = t0 + r;
+        const int64_t i = i0 + tx;
+        tile[r][tx] = (t < D.k && i < D.len) ? D.X[(size_t)t * D.len + i] : 0.0f;
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {
+        const int64_t i = i0 + r;
+        const uint32_t t = t0 + tx;
+        if (i < D.len && t < D.kp) D.Y[(size_t)i * D.kp + t] = tile[tx][r];
     }
 }
 

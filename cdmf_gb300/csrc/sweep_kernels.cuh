@@ -630,16 +630,16 @@ __global__ void __launch_bounds__(kBlock) flush_kernel(const uint32_t* __restric
 // order, (pred - v)^2 in double, NaN terms skipped but counted.  Fixed grid;
 // block partials in double; the last block adds them in block order and
 // writes sqrt(sum / nnz_test) and the NaN count.
+// Block `bid` of `nblk` blocks of one test-RMSE reduction.
 template <class VT>
-__global__ void __launch_bounds__(kBlock) rmse_kernel(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
-                                                      const VT* __restrict__ val, int64_t nt,
-                                                      const float* __restrict__ W, const float* __restrict__ H,
-                                                      int64_t m, int64_t n, uint32_t k, double* part,
-                                                      uint32_t* counter, double* out,
-                                                      unsigned long long* nan_out) {
+__device__ __forceinline__ void rmse_body(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
+                                          const VT* __restrict__ val, int64_t nt, const float* __restrict__ W,
+                                          const float* __restrict__ H, int64_t m, int64_t n, uint32_t k, double* part,
+                                          uint32_t* counter, double* out, unsigned long long* nan_out, uint32_t bid,
+                                          uint32_t nblk) {
     double acc = 0.0;
     unsigned nans = 0;
-    for (int64_t e = (int64_t)blockIdx.x * kBlock + threadIdx.x; e < nt; e += (int64_t)gridDim.x * kBlock) {
+    for (int64_t e = (int64_t)bid * kBlock + threadIdx.x; e < nt; e += (int64_t)nblk * kBlock) {
         const uint32_t i = row[e], j = col[e];
         double pred = 0.0;
         for (uint32_t t = 0; t < k; ++t)
@@ -666,19 +666,60 @@ __global__ void __launch_bounds__(kBlock) rmse_kernel(const uint32_t* __restrict
         double s = sm[0];
         unsigned long long c = smn[0];
         for (int q = 1; q < kWarps; ++q) { s = __dadd_rn(s, sm[q]); c += smn[q]; }
-        part[blockIdx.x] = s;
+        part[bid] = s;
         if (nan_out && c) atomicAdd(nan_out, c);
         __threadfence();
-        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+        last = (atomicAdd(counter, 1u) == nblk - 1);
     }
     __syncthreads();
     if (last && threadIdx.x == 0) {
         __threadfence();
         double s = 0.0;
-        for (uint32_t q = 0; q < gridDim.x; ++q) s = __dadd_rn(s, __ldcg(part + q));
+        for (uint32_t q = 0; q < nblk; ++q) s = __dadd_rn(s, __ldcg(part + q));
         *out = sqrt(s / (double)nt);
         *counter = 0;
     }
+}
+
+template <class VT>
+__global__ void __launch_bounds__(kBlock) rmse_kernel(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
+                                                      const VT* __restrict__ val, int64_t nt,
+                                                      const float* __restrict__ W, const float* __restrict__ H,
+                                                      int64_t m, int64_t n, uint32_t k, double* part,
+                                                      uint32_t* counter, double* out,
+                                                      unsigned long long* nan_out) {
+    rmse_body<VT>(row, col, val, nt, W, H, m, n, k, part, counter, out, nan_out, blockIdx.x, gridDim.x);
+}
+
+// Block index b of a grouped launch over nprob problems whose block ranges
+// are concatenated: the problem q with prefix[q] <= b < prefix[q + 1].
+__device__ __forceinline__ uint32_t group_of(const uint32_t* __restrict__ prefix, uint32_t nprob, uint32_t b) {
+    uint32_t lo = 0, hi = nprob;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (prefix[mid] <= b) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// Test RMSE of many problems in one launch.
+struct RmseDesc {
+    const uint32_t *row, *col;
+    const float* val;
+    int64_t nt, m, n;
+    const float *W, *H;
+    uint32_t k;
+    double* part;
+    uint32_t* counter;
+    double* out;
+};
+
+static __global__ void __launch_bounds__(kBlock) grouped_rmse_kernel(const RmseDesc* __restrict__ descs,
+                                                              const uint32_t* __restrict__ prefix, uint32_t nprob) {
+    const uint32_t q = group_of(prefix, nprob, blockIdx.x);
+    const RmseDesc D = descs[q];
+    rmse_body<float>(D.row, D.col, D.val, D.nt, D.W, D.H, D.m, D.n, D.k, D.part, D.counter, D.out, nullptr,
+                     blockIdx.x - prefix[q], prefix[q + 1] - prefix[q]);
 }
 
 }  // namespace cdmf
