@@ -302,12 +302,11 @@ __device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, 
 constexpr int kChunks = CDMF_CHUNKS;   // vector layout: 4-element chunks in flight per lane
 constexpr int kIlp = CDMF_ILP;         // interleaved layout: elements in flight per lane
 
-#ifndef CDMF_INTERLEAVED_STREAMS
 // Vector layout (default; measured faster for 16-bit residuals): lane takes 4 consecutive nonzeros per 128-bit load, after a
 // scalar head that reaches a 4-aligned position, then a scalar tail.
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
-__device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
-                                        float dj, float& gs, float& hs) {
+__device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
+                                            float dj, float& gs, float& hs) {
     Acc<KAHAN> g, h;
     uint32_t vbeg = (beg + 3u) & ~3u;
     if (vbeg > end) vbeg = end;
@@ -356,14 +355,14 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
     gs = g.value();
     hs = h.value();
 }
-#else
-// Interleaved layout (CDMF_INTERLEAVED_STREAMS): lane takes nonzeros beg+lane, beg+lane+S, ... so that
+// Interleaved layout: lane takes nonzeros beg+lane, beg+lane+S, ... so that
 // the S lanes of one load, and of the gather that follows it, touch S
 // consecutive nonzeros -- neighbouring cross indices, few cache lines per
-// gather.  kIlp nonzeros per lane are in flight per step.
-template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
-__device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
-                                        float dj, float& gs, float& hs) {
+// gather.  ILP nonzeros per lane are in flight per step.
+template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN, int ILP = kIlp>
+__device__ __forceinline__ void strided_il(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
+                                           float dj, float& gs, float& hs) {
+    constexpr int kIlp = ILP;
     Acc<KAHAN> g, h;
     uint32_t q = beg + lane;
     for (; q + (uint32_t)S * (kIlp - 1) < end; q += (uint32_t)S * kIlp) {
@@ -386,7 +385,25 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
     gs = g.value();
     hs = h.value();
 }
+
+#ifndef CDMF_THREAD_UNROLL
+#define CDMF_THREAD_UNROLL 1
 #endif
+#ifndef CDMF_GROUP_IL
+#define CDMF_GROUP_IL 0
+#endif
+template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
+__device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
+                                        float dj, float& gs, float& hs) {
+#ifdef CDMF_INTERLEAVED_STREAMS
+    strided_il<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
+#else
+    if (CDMF_GROUP_IL > 0 && S == 8)
+        strided_il<RT, MODE, SUB, ADD, S, KAHAN, (CDMF_GROUP_IL > 0 ? CDMF_GROUP_IL : 1)>(A, beg, end, lane, bj, dj, gs, hs);
+    else
+        strided_vec<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
+#endif
+}
 
 template <int WIDTH = 32>
 __device__ __forceinline__ void warp_sum2(float& g, float& h) {
@@ -539,7 +556,27 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
     }
     Acc<false> g, h;
     h.s = __fmul_rn(A.lambda, __uint2float_rn(len));         // h starts at lambda*nnz (src/cdmf_ref.cpp:8)
-    for (uint32_t q = beg; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
+    uint32_t q = beg;
+#if CDMF_THREAD_UNROLL > 1
+    // loads of CDMF_THREAD_UNROLL nonzeros in flight; sums still in index order
+    for (; q + CDMF_THREAD_UNROLL <= end; q += CDMF_THREAD_UNROLL) {
+        uint32_t iv[CDMF_THREAD_UNROLL];
+        float r[CDMF_THREAD_UNROLL];
+#pragma unroll
+        for (int e = 0; e < CDMF_THREAD_UNROLL; ++e) {
+            iv[e] = __ldcs(A.idx + q + e);
+            r[e] = Res<RT>::ld(A.res, q + e);
+        }
+#pragma unroll
+        for (int e = 0; e < CDMF_THREAD_UNROLL; ++e) {
+            float a, c, y;
+            fetch<MODE>(A, iv[e], a, c, y);
+            if (SUB || ADD) r[e] = Res<RT>::st(A.res, q + e, update<SUB, ADD>(r[e], a, c, bj, dj));
+            accumulate(g, h, y, r[e]);
+        }
+    }
+#endif
+    for (; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
     write_line<MODE>(A, j, __fdiv_rn(g.s, h.s), bj, dj);
 }
 
