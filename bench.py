@@ -346,22 +346,27 @@ def bench_batch(args, threads):
     runs = [sp["run"] for sp in specs]
     W0s = [synth.initial_w(r["k"], R.m, seed=q) for q, (R, r) in enumerate(zip(probs, runs))]
     n_outer = 10
-    with engine.Batch(probs, runs, maxiter=n_outer, maxinneriter=1, residual=args.residual, use_graph=True) as b:
+    with engine.Batch(probs, runs, maxiter=n_outer, maxinneriter=1, residual=args.residual,
+                      use_graph=bool(args.graph)) as b:
         for _ in range(args.warmup):
             b.set_factors(W0s)
             b.run(n_outer)
         t_batch, t_seq = [], []
+        rs = None
         with ClockSampler(0) as clk:
             for _ in range(args.steps):
                 b.set_factors(W0s)
                 rm = b.run(n_outer)
                 st = b.stats()
                 t_batch.append(st["train_ms"])
+                if args.quick:   # batched runs only (profiling)
+                    continue
                 b.set_factors(W0s)
                 rs, ms = b.run_sequential(n_outer)
                 t_seq.append(ms)
     updates = sum(r["k"] for r in runs) * n_outer
-    tb, tsq = statistics.median(t_batch), statistics.median(t_seq)
+    tb = statistics.median(t_batch)
+    tsq = statistics.median(t_seq) if t_seq else None
     line = {
         "metric": "batched CCD++ rank-one updates/s (64 uneven problems)", "value": updates / (tb / 1e3),
         "unit": "rank-one updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -370,8 +375,8 @@ def bench_batch(args, threads):
         "data": "synthetic (seeded): m logU[1k,200k], n logU[500,20k], nnz logU[50k,5M] <= 30% fill",
         "config": {"workload": "batch64", "problems": 64, "total_train_nnz": int(sum(R.nnz for R in probs)),
                    "outer": n_outer, "inner": 1, "step": "one batched run of 10 outer iterations"},
-        "sequential_ms": tsq, "speedup_vs_sequential": tsq / tb,
-        "rmse_equal_to_sequential": bool(np.array_equal(rm, rs)),
+        "sequential_ms": tsq, "speedup_vs_sequential": tsq / tb if tsq else None,
+        "rmse_equal_to_sequential": bool(np.array_equal(rm, rs)) if rs is not None else None,
         "gpu_launches": st["launches"], "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
