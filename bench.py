@@ -180,6 +180,7 @@ def main():
                     help="1/2: row-length-binned sweeps, 3: nonzero-balanced tiles")
     ap.add_argument("--graph", type=int, default=1, help="replay outer iterations from CUDA graphs")
     ap.add_argument("--relabel", type=int, default=1, help="renumber rows and columns by degree inside the engine")
+    ap.add_argument("--autotune", type=int, default=0, help="pick the bin thresholds by timing at create")
     ap.add_argument("--layout", default="lines", choices=["lines", "blocked"],
                     help="residual copy layout: lines (binned sweeps) or blocked (shared-memory gather tables)")
     ap.add_argument("--e2e-outer", type=int, default=20)
@@ -241,8 +242,9 @@ def main():
         t_create = time.perf_counter()
         e = engine.Engine(R, k, lam, maxiter=max(args.steps, args.e2e_outer), maxinneriter=T, residual=residual,
                           device=device, version=args.version, use_graph=bool(args.graph),
-                          relabel=bool(args.relabel), layout=args.layout)
+                          relabel=bool(args.relabel), layout=args.layout, autotune=bool(args.autotune))
         t_create = time.perf_counter() - t_create
+        bincfg = e.bincfg()
         e.set_factors(W0)
         e.run(args.warmup)
         dist.barrier()
@@ -265,7 +267,7 @@ def main():
                     achieved=bytes_launch / mean_launch_s / 1e9, bytes_launch=bytes_launch,
                     mean_launch_s=mean_launch_s, test_rmse=float(rm[-1]) if rm is not None else None,
                     clocks=clk.summary(), refresh_ms_per_outer=sp["refresh_ms"] / 2, rmse_ms_per_outer=sp["rmse_ms"] / 2,
-                    create_s=t_create)
+                    create_s=t_create, bincfg=bincfg)
 
     head = measure(args.residual)
     comp = measure(args.compare) if args.compare != "none" else None
@@ -305,7 +307,7 @@ def main():
         "config": {"workload": f"{WORKLOAD} {R.m}x{R.n} train_nnz={R.nnz} test_nnz={R.nnz_test} k={k} "
                                f"lambda={lam} T={T}",
                    "residual": args.residual, "version": args.version, "cuda_graph": bool(args.graph),
-                   "relabel": bool(args.relabel), "layout": args.layout,
+                   "relabel": bool(args.relabel), "layout": args.layout, "autotune": bool(args.autotune),
                    "step": "one outer iteration (k rank-one updates + test RMSE)",
                    "l2": "no flush: the residual copies streamed every feature exceed L2",
                    "parallelism": f"replicas x{ws}"},
@@ -330,6 +332,7 @@ def main():
         line["mixed_vs_fp32"] = value / comp["value"] if args.compare == "f32" else None
     line["refresh_ms_per_outer"] = head["refresh_ms_per_outer"]
     line["create_s"] = head["create_s"]
+    line["bincfg"] = head["bincfg"]
     if fmt is not None:
         line["formats"] = fmt
     line["rmse_ms_per_outer"] = head["rmse_ms_per_outer"]

@@ -84,12 +84,21 @@ struct DevBins {
 };
 
 // Bin thresholds (line length in nonzeros).
+#ifndef CDMF_GROUP_MAX
+#define CDMF_GROUP_MAX 256
+#endif
+#ifndef CDMF_WARP_MAX
+#define CDMF_WARP_MAX 2048
+#endif
+#ifndef CDMF_CTA_MAX
+#define CDMF_CTA_MAX 16384
+#endif
 struct BinCfg {
-    uint32_t thread_max = 12;    // <= : one thread per line
-    uint32_t group_max = 256;    // <= : one 8-lane group per line
-    uint32_t warp_max = 2048;    // <= : one warp per line
-    uint32_t cta_max = 16384;    // <= : one CTA per line; above: split
-    uint32_t chunk = 8192;       // nonzeros per chunk of a split line
+    uint32_t thread_max = 12;               // <= : one thread per line
+    uint32_t group_max = CDMF_GROUP_MAX;    // <= : one 8-lane group per line
+    uint32_t warp_max = CDMF_WARP_MAX;      // <= : one warp per line
+    uint32_t cta_max = CDMF_CTA_MAX;        // <= : one CTA per line; above: split
+    uint32_t chunk = 8192;                  // nonzeros per chunk of a split line
 };
 
 Bins plan_bins(const uint32_t* ptr, int64_t lines, bool sequential, const BinCfg& cfg) {
