@@ -202,13 +202,15 @@ def test_state_roundtrip_continues_identically():
 
 @pytest.mark.parametrize("version", [1, 3])
 def test_split_lines_within_fp32_budget(version):
-    # a matrix with very long columns exercises the split-line bin (> 16384 nnz)
+    # a matrix with very long columns exercises the split-line bin (lines
+    # above cta_max = 16384 here, set explicitly)
     R = synth.generate(m=60000, n=40, nnz_total=900000, test_fraction=0.01, row_alpha=0.5, row_min=1, row_max=40,
                        col_alpha=0.3, col_cap=60000, rank=4, seed=21)
     W0 = synth.initial_w(4, R.m, seed=1)
     ref = oracle.ccdpp(R, W0, 4, 0.05, 2, 2, threads=8, history=True)
     r64 = oracle.ccdpp(R, W0.astype(np.float64), 4, 0.05, 2, 2, threads=8, dtype=np.float64, history=True)
     with engine.Engine(R, 4, 0.05, 2, 2, version=version) as e:
+        e.set_bincfg(cta_max=16384)
         c, _ = e.bins("csc")
         assert c[4] > 0, c
         e.set_factors(W0)

@@ -16,8 +16,8 @@ SUM_RTOL = 1e-5   # FP32 tree sums: bound relative to the sum of |terms|
 
 def _matrix(seed=0):
     rng = np.random.default_rng(seed)
-    n = 20000
-    lens = np.concatenate([[40000, 0, 17000], rng.integers(2049, 6000, 6), rng.integers(257, 2048, 40),
+    n = 120000
+    lens = np.concatenate([[90000, 0, 17000], rng.integers(4097, 9000, 6), rng.integers(257, 4096, 40),
                            rng.integers(13, 256, 400), rng.integers(1, 12, 3000), np.zeros(50, np.int64)])
     rng.shuffle(lens)
     rows = np.repeat(np.arange(lens.size), lens)
