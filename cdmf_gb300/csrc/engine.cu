@@ -84,18 +84,29 @@ struct DevBins {
 };
 
 // Bin thresholds (line length in nonzeros).
-// Default bin thresholds.  Measured on the Netflix-shaped matrix (BF16):
-// warp lines up to 4096 and CTA lines up to 65536 give +7 % over 2048 / 16384;
-// the 64-problem batch loses 2 % with them (its small problems have few long
-// lines, which then fill too few warps).  cdmf_cuda_autotune picks per matrix.
+// Bin thresholds when the caller sets none.  Large matrices (the line
+// counts fill the GPU with warps) keep long lines on one warp: on the
+// Netflix-shaped matrix (99M nonzeros, BF16) warp lines up to 8192 and CTA
+// lines up to 65536 measured +10 % over 2048 / 16384.  Small matrices keep
+// 2048 / 16384: on the 64-problem batch (50k-5M nonzeros each) the larger
+// thresholds measured -2 % batched and -21 % one problem after another, as
+// their few long lines then fill too few warps.  cdmf_cuda_autotune picks per
+// matrix.
+constexpr int64_t kLargeNnz = 16 << 20;
 #ifndef CDMF_GROUP_MAX
 #define CDMF_GROUP_MAX 256
 #endif
 #ifndef CDMF_WARP_MAX
-#define CDMF_WARP_MAX 4096
+#define CDMF_WARP_MAX 2048
 #endif
 #ifndef CDMF_CTA_MAX
-#define CDMF_CTA_MAX 65536
+#define CDMF_CTA_MAX 16384
+#endif
+#ifndef CDMF_WARP_MAX_LARGE
+#define CDMF_WARP_MAX_LARGE 8192
+#endif
+#ifndef CDMF_CTA_MAX_LARGE
+#define CDMF_CTA_MAX_LARGE 65536
 #endif
 struct BinCfg {
     uint32_t thread_max = 12;               // <= : one thread per line
@@ -104,6 +115,15 @@ struct BinCfg {
     uint32_t cta_max = CDMF_CTA_MAX;        // <= : one CTA per line; above: split
     uint32_t chunk = 8192;                  // nonzeros per chunk of a split line
 };
+
+BinCfg default_bins(int64_t nnz) {
+    BinCfg c;
+    if (nnz >= kLargeNnz) {
+        c.warp_max = CDMF_WARP_MAX_LARGE;
+        c.cta_max = CDMF_CTA_MAX_LARGE;
+    }
+    return c;
+}
 
 Bins plan_bins(const uint32_t* ptr, int64_t lines, bool sequential, const BinCfg& cfg) {
     Bins B;
@@ -1308,6 +1328,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
             return bail(CDMF_ERR_CUDA);
     }
     h->seq = seq;
+    h->cfg = default_bins(N);
     if (relabel_on_gpu) {
         h->hptr_r = std::move(G.hptr_r);
         h->hptr_c = std::move(G.hptr_c);
@@ -2487,6 +2508,7 @@ int cdmf_spmv_as_csr5(cdmf_spmv* S) {
         CU(h, cudaStreamSynchronize(h->s));
         if (hb) return fail(h, CDMF_ERR_INVALID, "column index out of range");
     }
+    h->cfg = default_bins(h->nnz);
     const int r = upload_bins(h, h->csr, plan_bins(h->hptr_r.data(), h->m, false, h->cfg));
     if (r) return r;
     S->csr5 = true;
