@@ -102,6 +102,9 @@ constexpr int64_t kLargeNnz = 16 << 20;
 #ifndef CDMF_CTA_MAX
 #define CDMF_CTA_MAX 16384
 #endif
+#ifndef CDMF_SPLIT_CHUNK
+#define CDMF_SPLIT_CHUNK 8192
+#endif
 #ifndef CDMF_WARP_MAX_LARGE
 #define CDMF_WARP_MAX_LARGE 8192
 #endif
@@ -113,7 +116,7 @@ struct BinCfg {
     uint32_t group_max = CDMF_GROUP_MAX;    // <= : one 8-lane group per line
     uint32_t warp_max = CDMF_WARP_MAX;      // <= : one warp per line
     uint32_t cta_max = CDMF_CTA_MAX;        // <= : one CTA per line; above: split
-    uint32_t chunk = 8192;                  // nonzeros per chunk of a split line
+    uint32_t chunk = CDMF_SPLIT_CHUNK;      // nonzeros per chunk of a split line
 };
 
 BinCfg default_bins(int64_t nnz) {
