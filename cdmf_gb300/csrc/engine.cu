@@ -86,8 +86,9 @@ struct DevBins {
 // Bin thresholds (line length in nonzeros).
 // Bin thresholds when the caller sets none.  Large matrices (the line
 // counts fill the GPU with warps) keep long lines on one warp: on the
-// Netflix-shaped matrix (99M nonzeros, BF16) warp lines up to 8192 and CTA
-// lines up to 65536 measured +10 % over 2048 / 16384.  Small matrices keep
+// Netflix-shaped matrix (99M nonzeros, BF16) warp lines up to 16384, CTA
+// lines up to 65536 and split chunks of 16384 measured +11 % over 2048 /
+// 16384 / 8192.  Small matrices keep
 // 2048 / 16384: on the 64-problem batch (50k-5M nonzeros each) the larger
 // thresholds measured -2 % batched and -21 % one problem after another, as
 // their few long lines then fill too few warps.  cdmf_cuda_autotune picks per
@@ -106,7 +107,10 @@ constexpr int64_t kLargeNnz = 16 << 20;
 #define CDMF_SPLIT_CHUNK 8192
 #endif
 #ifndef CDMF_WARP_MAX_LARGE
-#define CDMF_WARP_MAX_LARGE 8192
+#define CDMF_WARP_MAX_LARGE 16384
+#endif
+#ifndef CDMF_SPLIT_CHUNK_LARGE
+#define CDMF_SPLIT_CHUNK_LARGE 16384
 #endif
 #ifndef CDMF_CTA_MAX_LARGE
 #define CDMF_CTA_MAX_LARGE 65536
@@ -124,6 +128,7 @@ BinCfg default_bins(int64_t nnz) {
     if (nnz >= kLargeNnz) {
         c.warp_max = CDMF_WARP_MAX_LARGE;
         c.cta_max = CDMF_CTA_MAX_LARGE;
+        c.chunk = CDMF_SPLIT_CHUNK_LARGE;
     }
     return c;
 }
