@@ -349,8 +349,10 @@ def bench_batch(args, threads):
     runs = [sp["run"] for sp in specs]
     W0s = [synth.initial_w(r["k"], R.m, seed=q) for q, (R, r) in enumerate(zip(probs, runs))]
     n_outer = 10
+    t_create = time.perf_counter()
     with engine.Batch(probs, runs, maxiter=n_outer, maxinneriter=1, residual=args.residual,
-                      use_graph=bool(args.graph)) as b:
+                      use_graph=bool(args.graph), autotune=bool(args.autotune)) as b:
+        t_create = time.perf_counter() - t_create
         for _ in range(args.warmup):
             b.set_factors(W0s)
             b.run(n_outer)
@@ -377,7 +379,9 @@ def bench_batch(args, threads):
         "dtype": f"{args.residual} residual, f32 factors and accumulation",
         "data": "synthetic (seeded): m logU[1k,200k], n logU[500,20k], nnz logU[50k,5M] <= 30% fill",
         "config": {"workload": "batch64", "problems": 64, "total_train_nnz": int(sum(R.nnz for R in probs)),
-                   "outer": n_outer, "inner": 1, "step": "one batched run of 10 outer iterations"},
+                   "outer": n_outer, "inner": 1, "step": "one batched run of 10 outer iterations",
+                   "autotune": bool(args.autotune)},
+        "create_s": t_create,
         "sequential_ms": tsq, "speedup_vs_sequential": tsq / tb if tsq else None,
         "rmse_equal_to_sequential": bool(np.array_equal(rm, rs)) if rs is not None else None,
         "gpu_launches": st["launches"], "clocks": clk.summary(),
