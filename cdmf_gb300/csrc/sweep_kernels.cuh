@@ -397,6 +397,11 @@ __device__ __forceinline__ void strided_il(const SweepArgs& A, uint32_t beg, uin
 #ifndef CDMF_GROUP_IL
 #define CDMF_GROUP_IL 0
 #endif
+// 8-lane group lines of at most CDMF_GROUP_SHORT nonzeros take the
+// interleaved layout, the whole line in flight at once (0 = off).
+#ifndef CDMF_GROUP_SHORT
+#define CDMF_GROUP_SHORT 0
+#endif
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
                                         float dj, float& gs, float& hs) {
@@ -405,6 +410,8 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
 #else
     if (CDMF_GROUP_IL > 0 && S == 8)
         strided_il<RT, MODE, SUB, ADD, S, KAHAN, (CDMF_GROUP_IL > 0 ? CDMF_GROUP_IL : 1)>(A, beg, end, lane, bj, dj, gs, hs);
+    else if (CDMF_GROUP_SHORT > 0 && S == 8 && end - beg <= CDMF_GROUP_SHORT)
+        strided_il<RT, MODE, SUB, ADD, S, KAHAN, (CDMF_GROUP_SHORT + 7) / 8>(A, beg, end, lane, bj, dj, gs, hs);
     else
         strided_vec<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
 #endif
