@@ -402,6 +402,7 @@ __device__ __forceinline__ void strided_il(const SweepArgs& A, uint32_t beg, uin
 #ifndef CDMF_GROUP_SHORT
 #define CDMF_GROUP_SHORT 0
 #endif
+constexpr int kGroupShortIlp = CDMF_GROUP_SHORT >= 32 ? 4 : CDMF_GROUP_SHORT > 8 ? (CDMF_GROUP_SHORT + 7) / 8 : 1;
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
                                         float dj, float& gs, float& hs) {
@@ -411,7 +412,7 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
     if (CDMF_GROUP_IL > 0 && S == 8)
         strided_il<RT, MODE, SUB, ADD, S, KAHAN, (CDMF_GROUP_IL > 0 ? CDMF_GROUP_IL : 1)>(A, beg, end, lane, bj, dj, gs, hs);
     else if (CDMF_GROUP_SHORT > 0 && S == 8 && end - beg <= CDMF_GROUP_SHORT)
-        strided_il<RT, MODE, SUB, ADD, S, KAHAN, (CDMF_GROUP_SHORT + 7) / 8>(A, beg, end, lane, bj, dj, gs, hs);
+        strided_il<RT, MODE, SUB, ADD, S, KAHAN, kGroupShortIlp>(A, beg, end, lane, bj, dj, gs, hs);
     else
         strided_vec<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
 #endif
