@@ -94,6 +94,10 @@ struct DevBins {
 // their few long lines then fill too few warps.  cdmf_cuda_autotune picks per
 // matrix.
 constexpr int64_t kLargeNnz = 16 << 20;
+// Small matrices also run 8-lane group lines of up to 32 nonzeros on the
+// interleaved layout (the whole line in flight): the 64-problem batch
+// measured 169 -> 161 ms; the Netflix-shaped matrix -1 %, so not there.
+constexpr uint32_t kGroupShort = 32;
 #ifndef CDMF_GROUP_MAX
 #define CDMF_GROUP_MAX 256
 #endif
@@ -495,6 +499,7 @@ SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const
     A.ngb = D.ngb;
     A.part = D.part;
     A.xcount = D.xcount;
+    A.group_short = h->nnz < kLargeNnz ? kGroupShort : 0;
     return A;
 }
 

@@ -97,6 +97,7 @@ struct SweepArgs {
     uint32_t* xcount;              // split-line arrival counters (left at 0)
     float* out2;                   // M_DUAL: sum of y^2 per line (out gets the sum of y * r)
     uint32_t ncross;               // M_CSRS: entries of the cross table (columns)
+    uint32_t group_short;          // 8-lane group lines up to this length: interleaved layout
 };
 
 // The cross table of an M_CSRS sweep, as three float planes (a | c | y) in
@@ -397,12 +398,9 @@ __device__ __forceinline__ void strided_il(const SweepArgs& A, uint32_t beg, uin
 #ifndef CDMF_GROUP_IL
 #define CDMF_GROUP_IL 0
 #endif
-// 8-lane group lines of at most CDMF_GROUP_SHORT nonzeros take the
-// interleaved layout, the whole line in flight at once (0 = off).
-#ifndef CDMF_GROUP_SHORT
-#define CDMF_GROUP_SHORT 0
-#endif
-constexpr int kGroupShortIlp = CDMF_GROUP_SHORT >= 32 ? 4 : CDMF_GROUP_SHORT > 8 ? (CDMF_GROUP_SHORT + 7) / 8 : 1;
+// 8-lane group lines of at most SweepArgs::group_short nonzeros take the
+// interleaved layout with the whole line in flight at once; longer ones the
+// vector layout.
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
                                         float dj, float& gs, float& hs) {
@@ -411,8 +409,8 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
 #else
     if (CDMF_GROUP_IL > 0 && S == 8)
         strided_il<RT, MODE, SUB, ADD, S, KAHAN, (CDMF_GROUP_IL > 0 ? CDMF_GROUP_IL : 1)>(A, beg, end, lane, bj, dj, gs, hs);
-    else if (CDMF_GROUP_SHORT > 0 && S == 8 && end - beg <= CDMF_GROUP_SHORT)
-        strided_il<RT, MODE, SUB, ADD, S, KAHAN, kGroupShortIlp>(A, beg, end, lane, bj, dj, gs, hs);
+    else if (S == 8 && end - beg <= A.group_short)
+        strided_il<RT, MODE, SUB, ADD, S, KAHAN, 4>(A, beg, end, lane, bj, dj, gs, hs);
     else
         strided_vec<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
 #endif
