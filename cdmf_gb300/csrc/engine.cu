@@ -313,7 +313,7 @@ int upload_bins(cdmf_handle* h, DevBins& D, Bins&& B) {
     D.ng = (uint32_t)B.g.size();
     D.nt = (uint32_t)B.t.size();
     D.nwb = (D.nw + kWarps - 1) / kWarps;
-    D.ngb = (D.ng + kBlock / 8 - 1) / (kBlock / 8);
+    D.ngb = (D.ng + kBlock / kGroupLanes - 1) / (kBlock / kGroupLanes);
     D.ntb = (D.nt + kBlock - 1) / kBlock;
     int r;
     if ((r = dalloc(h, &D.x, B.x.size())) || (r = dalloc(h, &D.c, B.c.size())) || (r = dalloc(h, &D.w, B.w.size())) ||

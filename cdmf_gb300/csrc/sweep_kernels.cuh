@@ -43,6 +43,10 @@ namespace cdmf {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
+#ifndef CDMF_GROUP_LANES
+#define CDMF_GROUP_LANES 8
+#endif
+constexpr int kGroupLanes = CDMF_GROUP_LANES;   // lanes per line in the group bin
 // Minimum resident blocks per SM asked of the compiler (register cap):
 // 6 blocks of 256 threads (at most 40 registers) measured best on the
 // 480,189 x 17,770 workload; 0 lets the compiler pick freely.
@@ -407,9 +411,9 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
 #ifdef CDMF_INTERLEAVED_STREAMS
     strided_il<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
 #else
-    if (CDMF_GROUP_IL > 0 && S == 8)
+    if (CDMF_GROUP_IL > 0 && S == kGroupLanes)
         strided_il<RT, MODE, SUB, ADD, S, KAHAN, (CDMF_GROUP_IL > 0 ? CDMF_GROUP_IL : 1)>(A, beg, end, lane, bj, dj, gs, hs);
-    else if (S == 8 && end - beg <= A.group_short)
+    else if (S == kGroupLanes && end - beg <= A.group_short)
         strided_il<RT, MODE, SUB, ADD, S, KAHAN, 4>(A, beg, end, lane, bj, dj, gs, hs);
     else
         strided_vec<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
@@ -533,16 +537,16 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
     }
     b -= A.nwb;
     if (b < A.ngb) {                                       // one line per 8-lane group
-        const uint32_t slot = b * (kBlock / 8) + (tid >> 3);
-        const uint32_t sub = tid & 7;
+        const uint32_t slot = b * (kBlock / kGroupLanes) + tid / kGroupLanes;
+        const uint32_t sub = tid % kGroupLanes;
         const bool valid = slot < A.ng;
         const uint32_t j = valid ? A.gl[slot] : 0u;
         const uint32_t beg = valid ? A.ptr[j] : 0u, end = valid ? A.ptr[j + 1] : 0u;
         float bj = 0.0f, dj = 0.0f;
         if (valid) line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
         float g = 0.0f, h = 0.0f;
-        strided<RT, MODE, SUB, ADD, 8, false>(A, beg, end, sub, bj, dj, g, h);
-        warp_sum2<8>(g, h);
+        strided<RT, MODE, SUB, ADD, kGroupLanes, false>(A, beg, end, sub, bj, dj, g, h);
+        warp_sum2<kGroupLanes>(g, h);
         if (valid && sub == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
         return;
     }
