@@ -94,6 +94,8 @@ struct DevBins {
 // their few long lines then fill too few warps.  cdmf_cuda_autotune picks per
 // matrix.
 constexpr int64_t kLargeNnz = 16 << 20;
+// Large matrices give group-bin lines 4 lanes (8 lines per warp): +2 % on the
+// Netflix-shaped matrix, -2 % on the 64-problem batch, which keeps 8.
 // Small matrices also run 8-lane group lines of up to 32 nonzeros on the
 // interleaved layout (the whole line in flight): the 64-problem batch
 // measured 169 -> 161 ms; the Netflix-shaped matrix -1 %, so not there.
@@ -224,6 +226,7 @@ struct cdmf_handle {
     uint32_t *d_row_old = nullptr, *d_col_old = nullptr;
     float* ftmp = nullptr;           // k * max(m, n) staging for the caller's factor order
     // narrow matrices: CSR sweeps gather from a shared-memory copy of Q
+    uint32_t group_lanes = 8;        // lanes per group-bin line (4 on large matrices)
     bool smemq = false;
     int sms = 0;
     uint32_t* smemq_queue = nullptr;
@@ -313,7 +316,8 @@ int upload_bins(cdmf_handle* h, DevBins& D, Bins&& B) {
     D.ng = (uint32_t)B.g.size();
     D.nt = (uint32_t)B.t.size();
     D.nwb = (D.nw + kWarps - 1) / kWarps;
-    D.ngb = (D.ng + kBlock / kGroupLanes - 1) / (kBlock / kGroupLanes);
+    const uint32_t per = kBlock / h->group_lanes;   // group lines per block
+    D.ngb = (D.ng + per - 1) / per;
     D.ntb = (D.nt + kBlock - 1) / kBlock;
     int r;
     if ((r = dalloc(h, &D.x, B.x.size())) || (r = dalloc(h, &D.c, B.c.size())) || (r = dalloc(h, &D.w, B.w.size())) ||
@@ -500,6 +504,7 @@ SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const
     A.part = D.part;
     A.xcount = D.xcount;
     A.group_short = h->nnz < kLargeNnz ? kGroupShort : 0;
+    A.group_lanes = h->group_lanes;
     return A;
 }
 
@@ -1342,6 +1347,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     }
     h->seq = seq;
     h->cfg = default_bins(N);
+    h->group_lanes = N >= kLargeNnz ? 4 : 8;
     if (relabel_on_gpu) {
         h->hptr_r = std::move(G.hptr_r);
         h->hptr_c = std::move(G.hptr_c);

@@ -32,7 +32,7 @@
 //                             in chunk order (deterministic, no float atomics)
 //   blocks [nx, nx+nc)        one line per CTA
 //   blocks [.., +nwb)         one line per warp
-//   blocks [.., +ngb)         one line per 8-lane group (4 lines per warp)
+//   blocks [.., +ngb)         one line per 4- or 8-lane group (8 or 4 lines per warp)
 //   blocks [.., +ntb)         one line per thread, index order = reference order
 #pragma once
 #include <cuda_bf16.h>
@@ -43,10 +43,6 @@ namespace cdmf {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
-#ifndef CDMF_GROUP_LANES
-#define CDMF_GROUP_LANES 8
-#endif
-constexpr int kGroupLanes = CDMF_GROUP_LANES;   // lanes per line in the group bin
 // Minimum resident blocks per SM asked of the compiler (register cap):
 // 6 blocks of 256 threads (at most 40 registers) measured best on the
 // 480,189 x 17,770 workload; 0 lets the compiler pick freely.
@@ -101,7 +97,8 @@ struct SweepArgs {
     uint32_t* xcount;              // split-line arrival counters (left at 0)
     float* out2;                   // M_DUAL: sum of y^2 per line (out gets the sum of y * r)
     uint32_t ncross;               // M_CSRS: entries of the cross table (columns)
-    uint32_t group_short;          // 8-lane group lines up to this length: interleaved layout
+    uint32_t group_short;          // group lines up to this length: interleaved layout
+    uint32_t group_lanes;          // lanes per group-bin line: 4 or 8
 };
 
 // The cross table of an M_CSRS sweep, as three float planes (a | c | y) in
@@ -411,9 +408,9 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
 #ifdef CDMF_INTERLEAVED_STREAMS
     strided_il<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
 #else
-    if (CDMF_GROUP_IL > 0 && S == kGroupLanes)
+    if (CDMF_GROUP_IL > 0 && S <= 8)
         strided_il<RT, MODE, SUB, ADD, S, KAHAN, (CDMF_GROUP_IL > 0 ? CDMF_GROUP_IL : 1)>(A, beg, end, lane, bj, dj, gs, hs);
-    else if (S == kGroupLanes && end - beg <= A.group_short)
+    else if (S <= 8 && end - beg <= A.group_short)
         strided_il<RT, MODE, SUB, ADD, S, KAHAN, 4>(A, beg, end, lane, bj, dj, gs, hs);
     else
         strided_vec<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
@@ -473,6 +470,22 @@ template <int MODE, bool SUB, bool ADD>
 __device__ __forceinline__ void line_scalars(const SweepArgs& A, uint32_t j, float& bj, float& dj) {
     bj = (SUB || MODE == M_CSC) && A.b ? A.b[j] : 0.0f;
     dj = (ADD || MODE == M_CSC) ? A.d[j] : 0.0f;
+}
+
+// Block b of the group bin: one line per L-lane group, kBlock / L lines.
+template <int RT, int MODE, bool SUB, bool ADD, int L>
+__device__ __forceinline__ void group_line(const SweepArgs& A, uint32_t b, uint32_t tid) {
+    const uint32_t slot = b * (kBlock / L) + tid / L;
+    const uint32_t sub = tid % L;
+    const bool valid = slot < A.ng;
+    const uint32_t j = valid ? A.gl[slot] : 0u;
+    const uint32_t beg = valid ? A.ptr[j] : 0u, end = valid ? A.ptr[j + 1] : 0u;
+    float bj = 0.0f, dj = 0.0f;
+    if (valid) line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
+    float g = 0.0f, h = 0.0f;
+    strided<RT, MODE, SUB, ADD, L, false>(A, beg, end, sub, bj, dj, g, h);
+    warp_sum2<L>(g, h);
+    if (valid && sub == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
 }
 
 // Work of block b of one sweep (b in [0, nx + nc + nwb + ngb + ntb)).
@@ -536,18 +549,9 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
         return;
     }
     b -= A.nwb;
-    if (b < A.ngb) {                                       // one line per 8-lane group
-        const uint32_t slot = b * (kBlock / kGroupLanes) + tid / kGroupLanes;
-        const uint32_t sub = tid % kGroupLanes;
-        const bool valid = slot < A.ng;
-        const uint32_t j = valid ? A.gl[slot] : 0u;
-        const uint32_t beg = valid ? A.ptr[j] : 0u, end = valid ? A.ptr[j + 1] : 0u;
-        float bj = 0.0f, dj = 0.0f;
-        if (valid) line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
-        float g = 0.0f, h = 0.0f;
-        strided<RT, MODE, SUB, ADD, kGroupLanes, false>(A, beg, end, sub, bj, dj, g, h);
-        warp_sum2<kGroupLanes>(g, h);
-        if (valid && sub == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
+    if (b < A.ngb) {                                       // one line per lane group
+        if (A.group_lanes == 4) group_line<RT, MODE, SUB, ADD, 4>(A, b, tid);
+        else group_line<RT, MODE, SUB, ADD, 8>(A, b, tid);
         return;
     }
     b -= A.ngb;
