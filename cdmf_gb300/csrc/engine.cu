@@ -94,8 +94,9 @@ struct DevBins {
 // their few long lines then fill too few warps.  cdmf_cuda_autotune picks per
 // matrix.
 constexpr int64_t kLargeNnz = 16 << 20;
-// Large matrices give group-bin lines 4 lanes (8 lines per warp): +2 % on the
-// Netflix-shaped matrix, -2 % on the 64-problem batch, which keeps 8.
+// Large matrices with a 16-bit residual give group-bin lines 4 lanes (8 lines
+// per warp): +2 % on the Netflix-shaped matrix at BF16, but -2 % at FP32 and
+// on the 64-problem batch, which keep 8.
 // Small matrices also run 8-lane group lines of up to 32 nonzeros on the
 // interleaved layout (the whole line in flight): the 64-problem batch
 // measured 169 -> 161 ms; the Netflix-shaped matrix -1 %, so not there.
@@ -1347,7 +1348,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     }
     h->seq = seq;
     h->cfg = default_bins(N);
-    h->group_lanes = N >= kLargeNnz ? 4 : 8;
+    h->group_lanes = N >= kLargeNnz && h->rt != 0 ? 4 : 8;
     if (relabel_on_gpu) {
         h->hptr_r = std::move(G.hptr_r);
         h->hptr_c = std::move(G.hptr_c);
