@@ -406,51 +406,3 @@ int gpu_relabel(const cdmf_problem& p, cudaStream_t s, GpuRelabel& out, std::vec
 }
 
 }  // namespace cdmf
-
-namespace {
-
-__global__ void iota_kernel(uint32_t* __restrict__ a, int64_t n) {
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-        a[q] = (uint32_t)q;
-}
-
-__global__ void gather_test(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ col,
-                            const float* __restrict__ val, int64_t n, uint32_t* __restrict__ col2,
-                            float* __restrict__ val2) {
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        col2[q] = col[perm[q]];
-        val2[q] = val[perm[q]];
-    }
-}
-
-}  // namespace
-
-namespace cdmf {
-
-int sort_test_by_row(uint32_t* row, uint32_t* col, float* val, int64_t nt, int64_t m, cudaStream_t s) {
-    if (nt < 2 || m < 2) return CDMF_OK;
-    Scratch S;
-    uint32_t *row2, *perm_in, *perm, *col2;
-    float* val2;
-    if (!S.get(&row2, nt) || !S.get(&perm_in, nt) || !S.get(&perm, nt) || !S.get(&col2, nt) || !S.get(&val2, nt))
-        return CDMF_ERR_ALLOC;
-#define RC(x) do { if ((x) != cudaSuccess) return CDMF_ERR_CUDA; } while (0)
-    iota_kernel<<<grid_for(nt), kThreads, 0, s>>>(perm_in, nt);
-    RC(cudaGetLastError());
-    const int bits = bits_for((uint64_t)m - 1);
-    size_t tb = 0;
-    RC(cub::DeviceRadixSort::SortPairs(nullptr, tb, row, row2, perm_in, perm, nt, 0, bits, s));
-    char* tmp = nullptr;
-    if (!S.get(&tmp, tb)) return CDMF_ERR_ALLOC;
-    RC(cub::DeviceRadixSort::SortPairs(tmp, tb, row, row2, perm_in, perm, nt, 0, bits, s));
-    gather_test<<<grid_for(nt), kThreads, 0, s>>>(perm, col, val, nt, col2, val2);
-    RC(cudaGetLastError());
-    RC(cudaMemcpyAsync(row, row2, 4 * (size_t)nt, cudaMemcpyDeviceToDevice, s));
-    RC(cudaMemcpyAsync(col, col2, 4 * (size_t)nt, cudaMemcpyDeviceToDevice, s));
-    RC(cudaMemcpyAsync(val, val2, 4 * (size_t)nt, cudaMemcpyDeviceToDevice, s));
-    RC(cudaStreamSynchronize(s));
-#undef RC
-    return CDMF_OK;
-}
-
-}  // namespace cdmf

@@ -1290,7 +1290,6 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         (r = up(h->te_val, p->test_val, 4 * h->nt)))
         return bail(r);
     if (cudaMemsetAsync(h->rmse_count, 0, 4, h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
-    if ((r = sort_test_by_row(h->te_row, h->te_col, h->te_val, h->nt, m, h->s))) return bail(r);
     phase("alloc+upload");
     const bool seq = o->reduce == CDMF_REDUCE_SEQUENTIAL;
     h->blocked = o->layout == 1 && !seq && N > 0;

@@ -30,9 +30,4 @@ struct GpuRelabel {
 // CDMF_OK or a CDMF_ERR_* status.  p must hold a valid CSR with nnz > 0.
 int gpu_relabel(const cdmf_problem& p, cudaStream_t s, GpuRelabel& out, std::vector<void*>& allocs);
 
-// Reorders a device test set by row (stable): the RMSE kernel's factor
-// gathers of neighbouring entries then share sectors.  The RMSE is a sum over
-// entries, so only its rounding order changes.
-int sort_test_by_row(uint32_t* row, uint32_t* col, float* val, int64_t nt, int64_t m, cudaStream_t s);
-
 }  // namespace cdmf
