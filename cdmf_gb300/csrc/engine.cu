@@ -228,6 +228,8 @@ struct cdmf_handle {
     float* ftmp = nullptr;           // k * max(m, n) staging for the caller's factor order
     // narrow matrices: CSR sweeps gather from a shared-memory copy of Q
     uint32_t group_lanes = 8;        // lanes per group-bin line (4 on large matrices)
+    uint16_t* csr_idx16 = nullptr;   // narrow matrices: the CSR column indices in 16 bits
+    bool idx16 = false;
     bool smemq = false;
     int sms = 0;
     uint32_t* smemq_queue = nullptr;
@@ -460,6 +462,7 @@ template <int RT>
 void launch_rt(const SweepArgs& A, int mode, bool sub, bool add, unsigned grid, cudaStream_t s) {
     if (mode == M_CSC) launch_mode<RT, M_CSC>(A, sub, add, grid, s);
     else if (mode == M_CSR) launch_mode<RT, M_CSR>(A, sub, add, grid, s);
+    else if (mode == M_CSR16) launch_mode<RT, M_CSR16>(A, sub, add, grid, s);
     else launch_mode<RT, M_PLAIN>(A, false, false, grid, s);
 }
 
@@ -582,12 +585,17 @@ int launch_blocked(cdmf_handle* h, int kind, const SweepArgs& A, int mode, bool 
     return CDMF_OK;
 }
 
+template <int RT, int MS>
+void smemq_attrs_ms(int bytes) {
+    cudaFuncSetAttribute(sweep_smemq_kernel<RT, true, true, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(sweep_smemq_kernel<RT, true, false, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(sweep_smemq_kernel<RT, false, true, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(sweep_smemq_kernel<RT, false, false, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
 template <int RT>
 void smemq_attrs(int bytes) {
-    cudaFuncSetAttribute(sweep_smemq_kernel<RT, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(sweep_smemq_kernel<RT, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(sweep_smemq_kernel<RT, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(sweep_smemq_kernel<RT, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    smemq_attrs_ms<RT, M_CSRS>(bytes);
+    smemq_attrs_ms<RT, M_CSRS16>(bytes);
 }
 
 // Whether the CSR sweeps of this matrix can stage Q in shared memory; sets
@@ -610,13 +618,19 @@ bool smemq_possible(int device, int64_t n, int* sms) {
     return true;
 }
 
-template <int RT>
-void smemq_rt(const SweepArgs& A, bool sub, bool add, unsigned grid, size_t smem, uint32_t nb, uint32_t* queue,
+template <int RT, int MS>
+void smemq_ms(const SweepArgs& A, bool sub, bool add, unsigned grid, size_t smem, uint32_t nb, uint32_t* queue,
               cudaStream_t s) {
-    if (sub && add) sweep_smemq_kernel<RT, true, true><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
-    else if (sub) sweep_smemq_kernel<RT, true, false><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
-    else if (add) sweep_smemq_kernel<RT, false, true><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
-    else sweep_smemq_kernel<RT, false, false><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
+    if (sub && add) sweep_smemq_kernel<RT, true, true, MS><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
+    else if (sub) sweep_smemq_kernel<RT, true, false, MS><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
+    else if (add) sweep_smemq_kernel<RT, false, true, MS><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
+    else sweep_smemq_kernel<RT, false, false, MS><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
+}
+template <int RT>
+void smemq_rt(const SweepArgs& A, bool i16, bool sub, bool add, unsigned grid, size_t smem, uint32_t nb,
+              uint32_t* queue, cudaStream_t s) {
+    if (i16) smemq_ms<RT, M_CSRS16>(A, sub, add, grid, smem, nb, queue, s);
+    else smemq_ms<RT, M_CSRS>(A, sub, add, grid, smem, nb, queue, s);
 }
 
 int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A, int mode, bool sub, bool add) {
@@ -628,9 +642,9 @@ int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A,
             Timed tm(h, kind);
             CU(h, cudaMemsetAsync(h->smemq_queue, 0, 4, h->s));
             switch (h->rt) {
-                case 0: smemq_rt<0>(A, sub, add, (unsigned)h->sms, smem, nb, h->smemq_queue, h->s); break;
-                case 1: smemq_rt<1>(A, sub, add, (unsigned)h->sms, smem, nb, h->smemq_queue, h->s); break;
-                default: smemq_rt<2>(A, sub, add, (unsigned)h->sms, smem, nb, h->smemq_queue, h->s); break;
+                case 0: smemq_rt<0>(A, h->idx16, sub, add, (unsigned)h->sms, smem, nb, h->smemq_queue, h->s); break;
+                case 1: smemq_rt<1>(A, h->idx16, sub, add, (unsigned)h->sms, smem, nb, h->smemq_queue, h->s); break;
+                default: smemq_rt<2>(A, h->idx16, sub, add, (unsigned)h->sms, smem, nb, h->smemq_queue, h->s); break;
             }
         }
         CU(h, cudaGetLastError());
@@ -670,6 +684,7 @@ int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A,
     }
     const unsigned grid = D.nx + D.nc + D.nwb + D.ngb + D.ntb;
     if (grid == 0) return CDMF_OK;
+    if (mode == M_CSR && h->idx16) mode = M_CSR16;
     {
         Timed tm(h, kind);
         switch (h->rt) {
@@ -713,6 +728,7 @@ void feature_args(cdmf_handle* h, uint32_t t, int it, SweepArgs& A, SweepArgs& B
     if (first) {
         B.Q = h->Q;
         B.ncross = (uint32_t)n;
+        B.idx16 = h->csr_idx16;
         B.b = Wp;
         B.d = Wt;
     } else {
@@ -895,6 +911,11 @@ int factors_out(cdmf_handle* h, const float* dev, float* user, int64_t len, cons
     CU(h, cudaGetLastError());
     CU(h, cudaMemcpyAsync(user, h->ftmp, bytes, cudaMemcpyDeviceToHost, h->s));
     return CDMF_OK;
+}
+
+__global__ void narrow_idx_kernel(const uint32_t* __restrict__ src, uint16_t* __restrict__ dst, int64_t count) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x)
+        dst[q] = (uint16_t)src[q];
 }
 
 __global__ void f32_to_res_kernel(const float* __restrict__ src, void* __restrict__ dst, int64_t count, int rt) {
@@ -1371,6 +1392,14 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         !std::getenv("CDMF_NO_SMEMQ")) {
         if ((r = dalloc(h, &h->smemq_queue, 1))) return bail(r);
         h->smemq = true;
+    }
+    // at most 65,536 columns: the first CSR sweep of each feature streams
+    // 16-bit column indices (6 bytes per nonzero instead of 8 at BF16)
+    if (!seq && !h->blocked && !h->tiles && N > 0 && n <= 65536 && !std::getenv("CDMF_NO_IDX16")) {
+        if ((r = dalloc(h, &h->csr_idx16, N))) return bail(r);
+        narrow_idx_kernel<<<1216, kBlock, 0, h->s>>>(h->csr_idx, h->csr_idx16, N);
+        if (cudaGetLastError() != cudaSuccess) return bail(CDMF_ERR_CUDA);
+        h->idx16 = true;
     }
     // fresh state: W := 0 until set, H := 0, residual := ratings
     if (cudaMemsetAsync(h->W, 0, sizeof(float) * k * m, h->s) != cudaSuccess ||

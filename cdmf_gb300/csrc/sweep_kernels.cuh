@@ -64,6 +64,11 @@ constexpr int M_CSC = 1;    // first CSC sweep of a feature: P gathers, emits Q
 constexpr int M_CSR = 2;    // first CSR sweep of a feature: Q gathers
 constexpr int M_DUAL = 3;   // dual SpMV (CSR5-style front end): y gathers, raw sums out
 constexpr int M_CSRS = 4;   // M_CSR with the cross table staged in shared memory (narrow matrices)
+constexpr int M_CSR16 = 5;  // M_CSR reading 16-bit column indices (at most 65,536 columns)
+constexpr int M_CSRS16 = 6; // M_CSRS reading 16-bit column indices
+template <int MODE> constexpr bool kIdx16 = MODE == M_CSR16 || MODE == M_CSRS16;
+template <int MODE> constexpr bool kCsrFirst = MODE == M_CSR || MODE == M_CSR16;
+template <int MODE> constexpr bool kCsrShared = MODE == M_CSRS || MODE == M_CSRS16;
 
 struct XTask {            // one chunk of a split line
     uint32_t line, beg, end, slot;
@@ -99,6 +104,7 @@ struct SweepArgs {
     uint32_t ncross;               // M_CSRS: entries of the cross table (columns)
     uint32_t group_short;          // group lines up to this length: interleaved layout
     uint32_t group_lanes;          // lanes per group-bin line: 4 or 8
+    const uint16_t* __restrict__ idx16;   // M_CSR16 / M_CSRS16: the column indices, 16 bits each
 };
 
 // The cross table of an M_CSRS sweep, as three float planes (a | c | y) in
@@ -252,12 +258,12 @@ __device__ __forceinline__ void fetch(const SweepArgs& A, uint32_t i, float& a, 
         a = p.x;
         c = p.y;
         y = p.y;
-    } else if (MODE == M_CSR) {
+    } else if (kCsrFirst<MODE>) {
         const float4 q = __ldg(A.Q + i);
         a = q.x;
         c = q.y;
         y = q.z;
-    } else if (MODE == M_CSRS) {
+    } else if (kCsrShared<MODE>) {
         a = cdmf_qsm[i];
         c = cdmf_qsm[A.ncross + i];
         y = cdmf_qsm[2 * A.ncross + i];
@@ -280,10 +286,27 @@ __device__ __forceinline__ void accumulate(AccT& g, AccT& h, float y, float r) {
     h.add(__fmul_rn(y, y));
 }
 
+// Index stream loads: one index, or the 4 indices at a 4-aligned position.
+template <int MODE>
+__device__ __forceinline__ uint32_t ld_idx1(const SweepArgs& A, uint32_t q) {
+    if (kIdx16<MODE>) return __ldcs(A.idx16 + q);
+    return __ldcs(A.idx + q);
+}
+template <int MODE>
+__device__ __forceinline__ void ld_idx4(const SweepArgs& A, uint32_t q, uint32_t (&iv)[4]) {
+    if (kIdx16<MODE>) {
+        const uint2 v = ld_stream2(A.idx16 + q);
+        iv[0] = v.x & 0xffffu; iv[1] = v.x >> 16; iv[2] = v.y & 0xffffu; iv[3] = v.y >> 16;
+    } else {
+        const uint4 v = ld_stream4(A.idx + q);
+        iv[0] = v.x; iv[1] = v.y; iv[2] = v.z; iv[3] = v.w;
+    }
+}
+
 // One scalar element: update, store, accumulate.
 template <int RT, int MODE, bool SUB, bool ADD, class AccT>
 __device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, float dj, AccT& g, AccT& h) {
-    const uint32_t i = __ldcs(A.idx + q);
+    const uint32_t i = ld_idx1<MODE>(A, q);
     float r = Res<RT>::ld(A.res, q);
     float a, c, y;
     fetch<MODE>(A, i, a, c, y);
@@ -320,8 +343,7 @@ __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, ui
         float r[kChunks][4];
 #pragma unroll
         for (int u = 0; u < kChunks; ++u) {
-            const uint4 v = ld_stream4(A.idx + q + 4u * S * u);
-            iv[u][0] = v.x; iv[u][1] = v.y; iv[u][2] = v.z; iv[u][3] = v.w;
+            ld_idx4<MODE>(A, q + 4u * S * u, iv[u]);
             Res<RT>::ld4(A.res, q + 4u * S * u, r[u]);
         }
 #pragma unroll
@@ -339,8 +361,8 @@ __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, ui
         }
     }
     for (; q < vend; q += 4u * S) {
-        const uint4 v = ld_stream4(A.idx + q);
-        const uint32_t iv[4] = {v.x, v.y, v.z, v.w};
+        uint32_t iv[4];
+        ld_idx4<MODE>(A, q, iv);
         float r[4], y[4];
         Res<RT>::ld4(A.res, q, r);
 #pragma unroll
@@ -372,7 +394,7 @@ __device__ __forceinline__ void strided_il(const SweepArgs& A, uint32_t beg, uin
         float r[kIlp], a[kIlp], c[kIlp], y[kIlp];
 #pragma unroll
         for (int u = 0; u < kIlp; ++u) {
-            iv[u] = __ldcs(A.idx + q + S * u);
+            iv[u] = ld_idx1<MODE>(A, q + S * u);
             r[u] = Res<RT>::ld(A.res, q + S * u);
         }
 #pragma unroll
@@ -583,7 +605,7 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
         float r[CDMF_THREAD_UNROLL];
 #pragma unroll
         for (int e = 0; e < CDMF_THREAD_UNROLL; ++e) {
-            iv[e] = __ldcs(A.idx + q + e);
+            iv[e] = ld_idx1<MODE>(A, q + e);
             r[e] = Res<RT>::ld(A.res, q + e);
         }
 #pragma unroll
@@ -609,7 +631,7 @@ __global__ void CDMF_SWEEP_BOUNDS sweep_kernel(const SweepArgs A) {
 // float planes, then its kSubs teams pull sweep blocks from a device work
 // queue and run them with every gather served from shared memory.  The
 // arithmetic is M_CSR's, element for element.
-template <int RT, bool SUB, bool ADD>
+template <int RT, bool SUB, bool ADD, int MS = M_CSRS>
 __global__ void __launch_bounds__(kBlock * kSubs, 1) sweep_smemq_kernel(const SweepArgs A, uint32_t nblocks,
                                                                       uint32_t* queue) {
     const uint32_t n = A.ncross;
@@ -628,7 +650,7 @@ __global__ void __launch_bounds__(kBlock * kSubs, 1) sweep_smemq_kernel(const Sw
         const uint32_t b = blk[sub];
         SubTeam::sync();
         if (b >= nblocks) return;
-        sweep_block<RT, M_CSRS, SUB, ADD, SubTeam>(A, b);
+        sweep_block<RT, MS, SUB, ADD, SubTeam>(A, b);
     }
 }
 

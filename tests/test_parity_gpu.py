@@ -464,3 +464,24 @@ def test_shared_memory_cross_table_matches_global(cpu_scale, residual, monkeypat
     assert np.array_equal(rm1, rm2)
     for key in ("W", "H", "res_csc", "res_csr"):
         assert np.array_equal(bits(s1[key]), bits(s2[key])), key
+
+
+@pytest.mark.parametrize("residual", ["f32", "bf16"])
+def test_sixteen_bit_column_indices_match(cpu_scale, residual, monkeypatch):
+    """Matrices with at most 65,536 columns stream 16-bit column indices in
+    the CSR sweeps; the result must equal the 32-bit path bit for bit
+    (CDMF_NO_IDX16 turns the narrow copy off at create)."""
+    R, run, W0, ref = cpu_scale
+    assert R.n <= 65536
+    out = []
+    for off in (False, True):
+        if off:
+            monkeypatch.setenv("CDMF_NO_IDX16", "1")
+        with engine.Engine(R, run["k"], run["lambda_"], 3, 1, residual=residual) as e:
+            e.set_factors(W0)
+            rm = e.run(3)
+            out.append((rm, e.state()))
+    (rm1, s1), (rm2, s2) = out
+    assert np.array_equal(rm1, rm2)
+    for key in ("W", "H", "res_csc", "res_csr"):
+        assert np.array_equal(bits(s1[key]), bits(s2[key])), key
