@@ -1919,6 +1919,9 @@ void grouped_rt(int mode, bool sub, bool add, const SweepArgs* d, const uint32_t
     prefer_l1(grouped_sweep_kernel<RT, M_CSC, false, true>);
     prefer_l1(grouped_sweep_kernel<RT, M_CSR, false, true>);
     prefer_l1(grouped_sweep_kernel<RT, M_PLAIN, false, false>);
+    prefer_l1(grouped_sweep_kernel<RT, M_CSR16, true, true>);
+    prefer_l1(grouped_sweep_kernel<RT, M_CSR16, true, false>);
+    prefer_l1(grouped_sweep_kernel<RT, M_CSR16, false, true>);
 #define CDMF_G(M, S, A) grouped_sweep_kernel<RT, M, S, A><<<grid, kBlock, 0, s>>>(d, pre, nq, queue)
     if (mode == M_PLAIN) CDMF_G(M_PLAIN, false, false);
     else if (mode == M_CSC) {
@@ -1926,6 +1929,11 @@ void grouped_rt(int mode, bool sub, bool add, const SweepArgs* d, const uint32_t
         else if (sub) CDMF_G(M_CSC, true, false);
         else if (add) CDMF_G(M_CSC, false, true);
         else CDMF_G(M_CSC, false, false);
+    } else if (mode == M_CSR16) {
+        if (sub && add) CDMF_G(M_CSR16, true, true);
+        else if (sub) CDMF_G(M_CSR16, true, false);
+        else if (add) CDMF_G(M_CSR16, false, true);
+        else CDMF_G(M_CSR16, false, false);
     } else {
         if (sub && add) CDMF_G(M_CSR, true, true);
         else if (sub) CDMF_G(M_CSR, true, false);
@@ -1941,6 +1949,7 @@ struct cdmf_batch {
     std::vector<cdmf_handle*> hs;
     cudaStream_t s = nullptr;
     int device = 0, rt = 0, T = 1, grid = 0, use_graph = 0;
+    bool all_idx16 = false;          // every problem has 16-bit CSR indices
     uint32_t kmax = 0;
     SweepArgs* d_desc = nullptr;
     SweepArgs* h_desc = nullptr;     // pinned staging
@@ -2181,10 +2190,11 @@ int execute_batch(cdmf_batch* B, const std::vector<BatchOp>& ops, const BatchPla
                 const SweepArgs* d = B->d_desc + op.desc_off;
                 const uint32_t* pre = B->d_prefix + op.prefix_off;
                 uint32_t* qu = B->d_queue + op.queue;
+                const int mode = op.mode == M_CSR && B->all_idx16 ? M_CSR16 : op.mode;
                 switch (B->rt) {
-                    case 0: grouped_rt<0>(op.mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
-                    case 1: grouped_rt<1>(op.mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
-                    default: grouped_rt<2>(op.mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
+                    case 0: grouped_rt<0>(mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
+                    case 1: grouped_rt<1>(mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
+                    default: grouped_rt<2>(mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
                 }
                 BCU(B, cudaGetLastError());
                 B->st.launches++;
@@ -2260,6 +2270,9 @@ int cdmf_cuda_batch_create(const cdmf_problem* probs, const cdmf_opts* opts, int
         B->hs.push_back(h);
         B->kmax = std::max(B->kmax, o.k);
     }
+    B->all_idx16 = !B->hs.empty();
+    for (cdmf_handle* h : B->hs)
+        if (!h->idx16) B->all_idx16 = false;
     int per_sm = 0, sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_sweep_kernel<0, M_CSR, true, true>, kBlock, 0);
