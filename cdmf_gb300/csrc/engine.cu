@@ -1413,7 +1413,10 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     const double T = std::max(1, o->maxinneriter);
     const double br = (double)h->rbytes;
     const double bi = h->blocked ? 2.0 : 4.0;   // index bytes as stored
-    h->st.bytes_per_update = T * 2.0 * N * (bi + br) + 2.0 * N * br + T * 4.0 * (m + n + 2) + 8.0 * (m + n);
+    // the first CSR sweep of a feature reads 16-bit indices when idx16 is on
+    const double bi_csr1 = h->idx16 ? 2.0 : bi;
+    h->st.bytes_per_update = T * N * (bi + br) + N * (bi_csr1 + br) + (T - 1) * N * (bi + br) + 2.0 * N * br +
+                             T * 4.0 * (m + n + 2) + 8.0 * (m + n);
     *out = h;
     return CDMF_OK;
 }
