@@ -83,6 +83,40 @@ def test_null_arguments():
     lib.cdmf_cuda_destroy(None)
 
 
+def test_new_entry_points_reject_bad_arguments_before_device_work():
+    """Argument checks of the format builder, the dual SpMV handle and the
+    objective monitor happen on the host, before any device is touched."""
+    lib = _lib.load()
+    n = ctypes.c_int64()
+    U, F, D = ctypes.c_uint32, ctypes.c_float, ctypes.c_double
+    z = np.zeros(4, np.uint32)
+    zf = np.zeros(4, np.float32)
+    zd = np.zeros(4, np.float64)
+    p = _lib.ptr
+    # negative sizes, missing outputs
+    assert lib.cdmf_cuda_compress(-1, 4, 0, None, None, None, 0, p(z, U), None, None, p(z, U), None, None,
+                                  ctypes.byref(n)) == -1
+    assert lib.cdmf_cuda_compress(3, 3, 2, p(z, U), p(z, U), p(zd, D), 0, None, p(z, U), p(zf, F), p(z, U),
+                                  p(z, U), p(zf, F), ctypes.byref(n)) == -1
+    # nonzeros with an empty dimension
+    assert lib.cdmf_cuda_compress(0, 3, 2, p(z, U), p(z, U), p(zd, D), 0, p(z, U), p(z, U), p(zf, F), p(z, U),
+                                  p(z, U), p(zf, F), ctypes.byref(n)) == -1
+    # beyond the 32-bit structure limits
+    assert lib.cdmf_cuda_compress(1 << 32, 3, 2, p(z, U), p(z, U), p(zd, D), 0, p(z, U), p(z, U), p(zf, F),
+                                  p(z, U), p(z, U), p(zf, F), ctypes.byref(n)) == -8
+    h = ctypes.c_void_p()
+    assert lib.cdmf_spmv_create(-1, 4, 0, ctypes.byref(h)) == -1
+    assert lib.cdmf_spmv_create(1 << 33, 4, 0, ctypes.byref(h)) == -8
+    assert lib.cdmf_spmv_create(4, 4, 0, None) == -1
+    for fn, args in (("cdmf_spmv_input_csr", (None, 0, None, None, None)), ("cdmf_spmv_as_csr5", (None,)),
+                     ("cdmf_spmv_as_csr", (None,)), ("cdmf_spmv_set_x", (None, None)),
+                     ("cdmf_spmv_run", (None, 1.0, None, None, None)),
+                     ("cdmf_cuda_objective", (None, None, None, None))):
+        assert getattr(lib, fn)(*args) == -1, fn
+    lib.cdmf_spmv_destroy(None)
+    assert lib.cdmf_spmv_last_error(None) == b""
+
+
 def test_anonymouslib_header_compiles_and_links(tmp_path):
     """The C++ face of the dual SpMV handle: a caller written against the
     reference's anonymouslibHandle calls compiles and links against the library."""
