@@ -196,6 +196,8 @@ def main():
     from cdmf_gb300 import synth
     threads = os.cpu_count() or 1
     if args.workload == "batch64" and args.impl == "cuda":
+        if rank != 0:   # one batch on one GPU; other ranks have nothing to add
+            return
         return bench_batch(args, threads)
 
     if args.impl == "reference":

@@ -1,0 +1,57 @@
+"""The multi-process path of bench.py on CPU (gloo, world size 2): the
+barrier and the max-over-ranks of the timings that bracket every timed
+region, and the replica arithmetic of the whole-job value.  The engine's
+path does not shard (one independent replica per GPU), so nothing else
+crosses ranks."""
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, ws, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE=str(ws), RANK=str(rank),
+                      LOCAL_RANK=str(rank))
+    sys.path.insert(0, ROOT)
+    import bench
+    d = bench.Dist(ws, rank)
+    d.barrier()
+    t_ms = d.max(10.0 + 5.0 * rank)          # rank 1 is the slower replica
+    d.barrier()
+    d.close()
+    # whole-job value of the replicas: every rank's updates over the slowest time
+    q.put((rank, t_ms, ws * 640 / (t_ms / 1e3)))
+
+
+def test_two_rank_barrier_max_and_value():
+    torch_mp = pytest.importorskip("torch.multiprocessing")
+    ctx = torch_mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(180)
+        assert p.exitcode == 0
+    res = sorted(q.get(timeout=30) for _ in range(2))
+    assert [r[1] for r in res] == [15.0, 15.0]
+    assert all(abs(r[2] - 2 * 640 / 0.015) < 1e-6 for r in res)
+
+
+def test_reference_arm_other_ranks_do_no_work():
+    env = dict(os.environ, RANK="1", LOCAL_RANK="1", WORLD_SIZE="2", MASTER_ADDR="127.0.0.1")
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2"],
+                       capture_output=True, text=True, timeout=120, env=env)
+    assert p.returncode == 0, p.stderr
+    assert p.stdout.strip() == ""
