@@ -22,9 +22,12 @@
 // feature writes P for the next feature as it finishes each row.
 //
 // Streams.  Inside a line, index and residual are read with 128-bit (16-bit
-// residual: 64-bit) vector loads, 4 nonzeros per lane per load, after a
-// scalar head that reaches a 4-element boundary; cache-streaming hints keep
-// them out of L1, which holds the gather tables.
+// residual or 16-bit column index: 64-bit) vector loads, 4 nonzeros per lane
+// per load, after a scalar head that reaches a 4-element boundary;
+// cache-streaming hints keep them out of L1, which holds the gather tables.
+// Matrices with at most 65,536 columns read 16-bit column indices in their
+// first CSR sweeps (M_CSR16, M_CSRS16).  Narrow matrices with an FP32
+// residual stage Q in shared memory for those sweeps (sweep_smemq_kernel).
 //
 // Lines are binned by length and all bins run in the same launch:
 //   blocks [0, nx)            one chunk of a split line (len > cta_max); the
