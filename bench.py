@@ -451,7 +451,10 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
     owners.append(ow)
     Hp, oh = _lib.pinned_empty((k, R.n), np.float32)
     owners.append(oh)
-    h2d = sum(getattr(Rp, f).nbytes for f in arrays) + W0.nbytes
+    # the engine copies the caller's CSC arrays only when it does not build
+    # the renumbered copies itself on the device (relabel off, or blocked)
+    copied = [f for f in arrays if not (f.startswith("csc_") and args.relabel and args.layout == "lines")]
+    h2d = sum(getattr(Rp, f).nbytes for f in copied) + W0.nbytes
     d2h = W0.nbytes + 4 * k * R.n + 8 * args.e2e_outer
     Wp[...] = W0
     kw = dict(residual=args.residual, device=device, version=args.version, use_graph=bool(args.graph),
