@@ -128,12 +128,16 @@ typedef struct cdmf_handle cdmf_handle;
 /* Called after every outer iteration: the reference's log-line values. */
 typedef void (*cdmf_outer_cb)(int oiter, double rmse, double train_ms_so_far, void* user);
 
+/* The reference's defaults (src/pmf.h:4-26: k 10, lambda 0.1, 5 x 5
+ * iterations, version 1) and the engine's for the rest. */
 void cdmf_opts_default(cdmf_opts* o);
 const char* cdmf_cuda_strerror(int status);
 int cdmf_cuda_version(void);
 
-/* One call = the reference engine call (cdmf_ocl_01 / cdmf_ocl_02 / cdmf_csr5):
- * upload, H := 0, maxiter outer iterations from the given W, download W and H.
+/* One call = the reference engine call (cdmf_ocl_01 / cdmf_ocl_02 / cdmf_csr5,
+ * src/cdmf.h:6-10, called at src/main.cpp:43,50,57): upload, H := 0
+ * (src/cdmf_ocl_1.cpp:64-68), maxiter outer iterations from the given W,
+ * download W and H.
  * rmse_out (nullable) receives maxiter values when opts->rmse_each_outer. */
 int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* H,
                     double* rmse_out, cdmf_outer_cb cb, void* user);
@@ -168,7 +172,10 @@ int cdmf_cuda_rmse_coo_noalloc(uint32_t k, int64_t m, int64_t n, const float* W,
                                const uint32_t* test_row, const uint32_t* test_col, const double* test_val,
                                void* stream, double* rmse, int64_t* nan_count);
 
-/* Handle API: the same engine split into upload / run / read-back. */
+/* Handle API: the same engine split into upload / run / read-back.  No single
+ * reference counterpart: the reference's engine functions (src/cdmf.h:6-10)
+ * do all of this in one call; the split serves one-step parity checks,
+ * repeated runs on one upload, and the benchmark. */
 int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** out);
 void cdmf_cuda_destroy(cdmf_handle* h);
 const char* cdmf_cuda_last_error(const cdmf_handle* h);
