@@ -27,7 +27,10 @@
 
 namespace cdmf {
 
-constexpr int kTileSteps = 16;
+#ifndef CDMF_TILE_STEPS
+#define CDMF_TILE_STEPS 16
+#endif
+constexpr int kTileSteps = CDMF_TILE_STEPS;
 constexpr int kWarpTile = 32 * kTileSteps;   // nonzeros per warp tile
 
 struct TileArgs {
