@@ -58,7 +58,7 @@ constexpr int kWarps = kBlock / 32;
 #define CDMF_SWEEP_BOUNDS __launch_bounds__(kBlock)
 #endif
 #ifndef CDMF_TILE_MIN_BLOCKS
-#define CDMF_TILE_MIN_BLOCKS 5
+#define CDMF_TILE_MIN_BLOCKS 6
 #endif
 
 // sweep modes
