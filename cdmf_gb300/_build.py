@@ -24,6 +24,10 @@ NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-fopenm
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-I", INC]
 
 CU_SOURCES = ["engine.cu", "noalloc.cu", "compress.cu"]
+# launch.cu holds the kernel launchers; it is compiled once per residual type
+# (0 = FP32, 1 = BF16, 2 = FP16) and kernel family (0 = binned sweeps, 1 =
+# tiles, blocks, batches, refresh), so the instantiations compile in parallel.
+CU_VARIANTS = [("launch.cu", rt, part) for rt in (0, 1, 2) for part in (0, 1)]
 CXX_SOURCES = ["synth.cpp", "relabel.cpp", "blocked.cpp"]
 CLI_SOURCES = ["cli/main.cpp", "cli/loader.cpp"]
 
@@ -55,6 +59,11 @@ def build(verbose=False, defines=(), lib_path=None, obj_dir=None, with_cli=True)
         obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
         cmds.append([NVCC] + NVFLAGS + dflags + ["-c", os.path.join(CSRC, src), "-o", obj])
         objs.append(obj)
+    for src, rt, part in CU_VARIANTS:
+        obj = os.path.join(obj_dir, "launch_rt%d_part%d.o" % (rt, part))
+        cmds.append([NVCC] + NVFLAGS + dflags + ["-DCDMF_LAUNCH_RT=%d" % rt, "-DCDMF_LAUNCH_PART=%d" % part,
+                                                 "-c", os.path.join(CSRC, src), "-o", obj])
+        objs.append(obj)
     for src in CXX_SOURCES:
         obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
         cmds.append(["g++"] + CXXFLAGS + ["-c", os.path.join(CSRC, src), "-o", obj])
@@ -72,7 +81,8 @@ def build(verbose=False, defines=(), lib_path=None, obj_dir=None, with_cli=True)
             print(" ".join(c), file=sys.stderr)
     _run_parallel(cmds)
     tmp = lib + ".tmp"
-    _run_parallel([[NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fopenmp", "-lgomp"]])
+    _run_parallel([[NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fopenmp", "-lgomp",
+                                                         "-Xlinker", "--no-undefined"]])
     os.replace(tmp, lib)
     if cli_objs:
         _run_parallel([["g++", "-o", CLI] + cli_objs + ["-L", LIBDIR, "-lcdmf_cuda", "-Wl,-rpath,$ORIGIN/../lib",

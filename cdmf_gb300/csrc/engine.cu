@@ -24,6 +24,7 @@
 #include "gpu_build.h"
 #include "tile_kernels.cuh"
 #include "blocked_kernels.cuh"
+#include "launch.h"
 #include "relabel.h"
 #include "blocked.h"
 
@@ -434,58 +435,6 @@ struct Timed {
     }
 };
 
-// The sweeps use almost no shared memory; give the unified L1/shared
-// storage to L1, which holds the gather tables.
-template <class K>
-void prefer_l1(K kernel) {
-    static std::mutex mu;
-    static std::set<const void*> done;
-    std::lock_guard<std::mutex> lk(mu);
-    if (done.insert((const void*)kernel).second)
-        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-}
-
-template <int RT, int MODE>
-void launch_mode(const SweepArgs& A, bool sub, bool add, unsigned grid, cudaStream_t s) {
-    prefer_l1(sweep_kernel<RT, MODE, true, true>);
-    prefer_l1(sweep_kernel<RT, MODE, true, false>);
-    prefer_l1(sweep_kernel<RT, MODE, false, true>);
-    prefer_l1(sweep_kernel<RT, MODE, false, false>);
-    if (MODE == M_PLAIN) sweep_kernel<RT, M_PLAIN, false, false><<<grid, kBlock, 0, s>>>(A);
-    else if (sub && add) sweep_kernel<RT, MODE, true, true><<<grid, kBlock, 0, s>>>(A);
-    else if (sub) sweep_kernel<RT, MODE, true, false><<<grid, kBlock, 0, s>>>(A);
-    else if (add) sweep_kernel<RT, MODE, false, true><<<grid, kBlock, 0, s>>>(A);
-    else sweep_kernel<RT, MODE, false, false><<<grid, kBlock, 0, s>>>(A);
-}
-
-template <int RT>
-void launch_rt(const SweepArgs& A, int mode, bool sub, bool add, unsigned grid, cudaStream_t s) {
-    if (mode == M_CSC) launch_mode<RT, M_CSC>(A, sub, add, grid, s);
-    else if (mode == M_CSR) launch_mode<RT, M_CSR>(A, sub, add, grid, s);
-    else if (mode == M_CSR16) launch_mode<RT, M_CSR16>(A, sub, add, grid, s);
-    else launch_mode<RT, M_PLAIN>(A, false, false, grid, s);
-}
-
-template <int RT, int MODE>
-void tile_mode(const TileArgs& T, bool sub, bool add, unsigned grid, cudaStream_t s) {
-    prefer_l1(tile_sweep_kernel<RT, MODE, true, true>);
-    prefer_l1(tile_sweep_kernel<RT, MODE, true, false>);
-    prefer_l1(tile_sweep_kernel<RT, MODE, false, true>);
-    prefer_l1(tile_sweep_kernel<RT, MODE, false, false>);
-    if (MODE == M_PLAIN) tile_sweep_kernel<RT, M_PLAIN, false, false><<<grid, kBlock, 0, s>>>(T);
-    else if (sub && add) tile_sweep_kernel<RT, MODE, true, true><<<grid, kBlock, 0, s>>>(T);
-    else if (sub) tile_sweep_kernel<RT, MODE, true, false><<<grid, kBlock, 0, s>>>(T);
-    else if (add) tile_sweep_kernel<RT, MODE, false, true><<<grid, kBlock, 0, s>>>(T);
-    else tile_sweep_kernel<RT, MODE, false, false><<<grid, kBlock, 0, s>>>(T);
-}
-
-template <int RT>
-void tile_rt(const TileArgs& T, int mode, bool sub, bool add, unsigned grid, cudaStream_t s) {
-    if (mode == M_CSC) tile_mode<RT, M_CSC>(T, sub, add, grid, s);
-    else if (mode == M_CSR) tile_mode<RT, M_CSR>(T, sub, add, grid, s);
-    else tile_mode<RT, M_PLAIN>(T, false, false, grid, s);
-}
-
 SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const uint32_t* idx, void* res) {
     SweepArgs A;
     std::memset(&A, 0, sizeof(A));
@@ -510,42 +459,6 @@ SweepArgs base_args(cdmf_handle* h, const DevBins& D, const uint32_t* ptr, const
     A.group_short = h->nnz < kLargeNnz ? kGroupShort : 0;
     A.group_lanes = h->group_lanes;
     return A;
-}
-
-// Opts a kernel into `bytes` of dynamic shared memory (beyond the default
-// 48 KB including static) with the unified storage split toward shared memory.
-template <class K>
-void allow_smem(K kernel, size_t bytes) {
-    static std::mutex mu;
-    static std::set<const void*> done;
-    std::lock_guard<std::mutex> lk(mu);
-    if (done.insert((const void*)kernel).second) {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    }
-}
-
-template <int RT, int MODE, bool SUB, bool ADD>
-void blocked_launch(const BlockedArgs& B, unsigned grid, cudaStream_t s) {
-    using T = typename Tbl<MODE>::T;
-    allow_smem(blocked_sweep_kernel<RT, MODE, SUB, ADD>, (size_t)kXbRow * sizeof(float4));
-    blocked_sweep_kernel<RT, MODE, SUB, ADD><<<grid, kBlock, B.xb * sizeof(T), s>>>(B);
-}
-
-template <int RT, int MODE>
-void blocked_mode(const BlockedArgs& B, bool sub, bool add, unsigned grid, cudaStream_t s) {
-    if (MODE == M_PLAIN) blocked_launch<RT, M_PLAIN, false, false>(B, grid, s);
-    else if (sub && add) blocked_launch<RT, MODE, true, true>(B, grid, s);
-    else if (sub) blocked_launch<RT, MODE, true, false>(B, grid, s);
-    else if (add) blocked_launch<RT, MODE, false, true>(B, grid, s);
-    else blocked_launch<RT, MODE, false, false>(B, grid, s);
-}
-
-template <int RT>
-void blocked_rt(const BlockedArgs& B, int mode, bool sub, bool add, unsigned grid, cudaStream_t s) {
-    if (mode == M_CSC) blocked_mode<RT, M_CSC>(B, sub, add, grid, s);
-    else if (mode == M_CSR) blocked_mode<RT, M_CSR>(B, sub, add, grid, s);
-    else blocked_mode<RT, M_PLAIN>(B, false, false, grid, s);
 }
 
 int launch_blocked(cdmf_handle* h, int kind, const SweepArgs& A, int mode, bool sub, bool add) {
@@ -585,19 +498,6 @@ int launch_blocked(cdmf_handle* h, int kind, const SweepArgs& A, int mode, bool 
     return CDMF_OK;
 }
 
-template <int RT, int MS>
-void smemq_attrs_ms(int bytes) {
-    cudaFuncSetAttribute(sweep_smemq_kernel<RT, true, true, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(sweep_smemq_kernel<RT, true, false, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(sweep_smemq_kernel<RT, false, true, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(sweep_smemq_kernel<RT, false, false, MS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-}
-template <int RT>
-void smemq_attrs(int bytes) {
-    smemq_attrs_ms<RT, M_CSRS>(bytes);
-    smemq_attrs_ms<RT, M_CSRS16>(bytes);
-}
-
 // Whether the CSR sweeps of this matrix can stage Q in shared memory; sets
 // the kernels' dynamic shared memory limit once per process and device.
 bool smemq_possible(int device, int64_t n, int* sms) {
@@ -616,21 +516,6 @@ bool smemq_possible(int device, int64_t n, int* sms) {
         smemq_attrs<2>(optin - 1024);
     }
     return true;
-}
-
-template <int RT, int MS>
-void smemq_ms(const SweepArgs& A, bool sub, bool add, unsigned grid, size_t smem, uint32_t nb, uint32_t* queue,
-              cudaStream_t s) {
-    if (sub && add) sweep_smemq_kernel<RT, true, true, MS><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
-    else if (sub) sweep_smemq_kernel<RT, true, false, MS><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
-    else if (add) sweep_smemq_kernel<RT, false, true, MS><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
-    else sweep_smemq_kernel<RT, false, false, MS><<<grid, kBlock * kSubs, smem, s>>>(A, nb, queue);
-}
-template <int RT>
-void smemq_rt(const SweepArgs& A, bool i16, bool sub, bool add, unsigned grid, size_t smem, uint32_t nb,
-              uint32_t* queue, cudaStream_t s) {
-    if (i16) smemq_ms<RT, M_CSRS16>(A, sub, add, grid, smem, nb, queue, s);
-    else smemq_ms<RT, M_CSRS>(A, sub, add, grid, smem, nb, queue, s);
 }
 
 int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A, int mode, bool sub, bool add) {
@@ -837,27 +722,29 @@ int flush_pending(cdmf_handle* h) {
     return CDMF_OK;
 }
 
-template <int RT, int NU>
-void launch_refresh_t(cdmf_handle* h, const float* pa, const float* pb) {
-    refresh_warp_kernel<RT, NU><<<h->ref_grid, kBlock, 0, h->s>>>(
-        h->csr_ptr, h->csr_idx, h->csr_val, h->ref_to_csr, h->to_csc, h->m, h->nnz, h->Wrm, h->Hrm, h->kp,
-        h->res_csr, h->res_csc, pa, pb, h->ref_part, h->ref_count, h->drift_out, h->nonfinite);
-}
-
-template <int RT>
-void launch_refresh_rt(cdmf_handle* h, int nu, const float* pa, const float* pb) {
-    switch (nu) {
-        case 1: launch_refresh_t<RT, 1>(h, pa, pb); break;
-        case 2: launch_refresh_t<RT, 2>(h, pa, pb); break;
-        case 4: launch_refresh_t<RT, 4>(h, pa, pb); break;
-        case 8: launch_refresh_t<RT, 8>(h, pa, pb); break;
-        default: launch_refresh_t<RT, 0>(h, pa, pb); break;
-    }
-}
-
 void launch_refresh(cdmf_handle* h, int rt, int nu, const float* pa, const float* pb) {
-    if (rt == 1) launch_refresh_rt<1>(h, nu, pa, pb);
-    else launch_refresh_rt<2>(h, nu, pa, pb);
+    RefreshDesc D;
+    D.ptr = h->csr_ptr;
+    D.idx = h->csr_idx;
+    D.val = h->csr_val;
+    D.to_csr = h->ref_to_csr;
+    D.to_csc = h->to_csc;
+    D.m = h->m;
+    D.nnz = h->nnz;
+    D.Wrm = h->Wrm;
+    D.Hrm = h->Hrm;
+    D.kp = h->kp;
+    D.slices = (uint32_t)nu;
+    D.res_csr = h->res_csr;
+    D.res_csc = h->res_csc;
+    D.pa = pa;
+    D.pb = pb;
+    D.part = h->ref_part;
+    D.counter = h->ref_count;
+    D.drift_out = h->drift_out;
+    D.nonfinite = h->nonfinite;
+    if (rt == 1) launch_refresh_rt<1>(D, (unsigned)h->ref_grid, h->s);
+    else launch_refresh_rt<2>(D, (unsigned)h->ref_grid, h->s);
 }
 
 // 16-bit modes: recompute both residual copies from the FP32 ratings and
@@ -1257,8 +1144,8 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         h->d_col_old = G.d_col_old;
         // the test set in the new numbering
         uvec<uint32_t> row_new(m), col_new(n);
-        for (int64_t q = 0; q < m; ++q) row_new[h->row_old[q]] = (uint32_t)q;
-        for (int64_t q = 0; q < n; ++q) col_new[h->col_old[q]] = (uint32_t)q;
+        for (int64_t v = 0; v < m; ++v) row_new[h->row_old[v]] = (uint32_t)v;
+        for (int64_t v = 0; v < n; ++v) col_new[h->col_old[v]] = (uint32_t)v;
         te_row.resize(p->nnz_test);
         te_col.resize(p->nnz_test);
 #pragma omp parallel for schedule(static)
@@ -1912,40 +1799,6 @@ struct BatchPlan {
     std::vector<RmseDesc> mdescs;
 };
 
-template <int RT>
-void grouped_rt(int mode, bool sub, bool add, const SweepArgs* d, const uint32_t* pre, uint32_t nq, uint32_t* queue,
-                int grid, cudaStream_t s) {
-    prefer_l1(grouped_sweep_kernel<RT, M_CSC, true, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR, true, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSC, true, false>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR, true, false>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSC, false, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR, false, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_PLAIN, false, false>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR16, true, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR16, true, false>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR16, false, true>);
-#define CDMF_G(M, S, A) grouped_sweep_kernel<RT, M, S, A><<<grid, kBlock, 0, s>>>(d, pre, nq, queue)
-    if (mode == M_PLAIN) CDMF_G(M_PLAIN, false, false);
-    else if (mode == M_CSC) {
-        if (sub && add) CDMF_G(M_CSC, true, true);
-        else if (sub) CDMF_G(M_CSC, true, false);
-        else if (add) CDMF_G(M_CSC, false, true);
-        else CDMF_G(M_CSC, false, false);
-    } else if (mode == M_CSR16) {
-        if (sub && add) CDMF_G(M_CSR16, true, true);
-        else if (sub) CDMF_G(M_CSR16, true, false);
-        else if (add) CDMF_G(M_CSR16, false, true);
-        else CDMF_G(M_CSR16, false, false);
-    } else {
-        if (sub && add) CDMF_G(M_CSR, true, true);
-        else if (sub) CDMF_G(M_CSR, true, false);
-        else if (add) CDMF_G(M_CSR, false, true);
-        else CDMF_G(M_CSR, false, false);
-    }
-#undef CDMF_G
-}
-
 }  // namespace
 
 struct cdmf_batch {
@@ -2278,7 +2131,7 @@ int cdmf_cuda_batch_create(const cdmf_problem* probs, const cdmf_opts* opts, int
         if (!h->idx16) B->all_idx16 = false;
     int per_sm = 0, sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_sweep_kernel<0, M_CSR, true, true>, kBlock, 0);
+    per_sm = grouped_blocks_per_sm();
     B->grid = std::max(1, sms) * std::max(1, per_sm);
     *out = B;
     return CDMF_OK;
@@ -2611,8 +2464,7 @@ int cdmf_spmv_run(cdmf_spmv* S, float alpha, float* y_t, float* y_b, double* ms)
     const unsigned grid = h->csr.nx + h->csr.nc + h->csr.nwb + h->csr.ngb + h->csr.ntb;
     CU(h, cudaEventRecord(h->ev_start, h->s));
     if (grid) {
-        prefer_l1(sweep_kernel<0, M_DUAL, false, false>);
-        sweep_kernel<0, M_DUAL, false, false><<<grid, kBlock, 0, h->s>>>(A);
+        launch_dual(A, grid, h->s);
         CU(h, cudaGetLastError());
     }
     CU(h, cudaEventRecord(h->ev_stop, h->s));
