@@ -1,0 +1,69 @@
+"""Generates tests/golden/workloads.json: the oracle's test-RMSE trajectories
+(FP32 = the reference's arithmetic, FP64 = the same algorithm in double) on
+the synthetic stand-ins for the reference's benchmark data sets, with
+checksums of the generated matrix and initial factors so a test knows the
+matrix it regenerates is the one the trajectories belong to.
+
+Workloads (cdmf_gb300.synth presets, W0 = synth.initial_w(k, m, seed=0), H = 0):
+  jester_shape   73,421 x 100, 4.2M nonzeros, k=10, lambda=0.5, 15 x 2
+  ml20m_shape    138,493 x 26,744, 19.6M nonzeros, k=128, lambda=0.1, 10 x 3
+  netflix_shape  480,189 x 17,770, 99.1M nonzeros, k=64, lambda=0.05, 20 x 1
+The oracle restatement is pinned bit for bit to the reference's own engine
+by make_golden.py; these trajectories are its output on larger inputs, too
+slow to recompute inside a GPU test (netflix_shape takes tens of minutes of
+CPU per precision).
+
+Usage: python tests/golden/make_workloads.py [workload ...]   (merges into the file)
+"""
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from cdmf_gb300 import synth  # noqa: E402
+from oracle import oracle  # noqa: E402
+
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "workloads.json")
+DEFAULT = ("jester_shape", "ml20m_shape", "netflix_shape")
+
+
+def bit_sum(a):
+    """Sum of the 32-bit patterns: exact and independent of summation order."""
+    return int(np.ascontiguousarray(a).view(np.uint32).astype(np.int64).sum())
+
+
+def checksums(R, W0):
+    """Sizes and bit-pattern sums that identify the generated inputs."""
+    return dict(m=int(R.m), n=int(R.n), nnz=int(R.nnz), nnz_test=int(R.te_val.size),
+                csr_idx_sum=bit_sum(R.csr_idx), csr_val_sum=bit_sum(R.csr_val), te_row_sum=bit_sum(R.te_row),
+                te_val_sum=bit_sum(R.te_val), w0_sum=bit_sum(W0))
+
+
+def make(name):
+    R, run = synth.config(name)
+    k, lam, T, it = run["k"], run["lambda_"], run["maxinneriter"], run["maxiter"]
+    W0 = synth.initial_w(k, R.m, seed=0)
+    out = dict(k=k, lam=lam, maxiter=it, maxinner=T, inputs=checksums(R, W0))
+    for dt, tag in ((np.float32, "f32"), (np.float64, "f64")):
+        t0 = time.time()
+        r = oracle.ccdpp(R, W0.astype(dt), k, lam, it, T, dtype=dt)
+        out["rmse_" + tag] = [float(x) for x in r["rmse"]]
+        print(f"{name} {tag}: {time.time() - t0:.1f} s, final RMSE {r['rmse'][-1]:.9f}", flush=True)
+    return out
+
+
+def main(names):
+    data = json.load(open(OUT)) if os.path.exists(OUT) else {}
+    for name in names:
+        data[name] = make(name)
+        with open(OUT, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+            f.write("\n")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:] or DEFAULT)

@@ -1,0 +1,87 @@
+"""The synthetic stand-ins for the reference's Jester and MovieLens-20M runs
+(their shapes, value distributions, k, lambda and outer x inner) through the
+engine, against the oracle's test-RMSE trajectories in
+tests/golden/workloads.json (FP32 = the reference's arithmetic, FP64 = the
+same algorithm in double), after every outer iteration:
+  - FP32 residual, tree order, versions 1 and 3: within the reference's own
+    FP32 error of the FP64 oracle, max(1e-5, 2 |rmse32 - rmse64|);
+  - FP16 residual: within 1e-3 of the FP64 oracle;
+  - BF16 residual: within 1e-3 of the FP64 oracle once the first refresh has
+    run (outer iteration 2 on); in outer iteration 1 the residual has gone
+    through k (k = 128 here) rank-one updates stored in BF16 with no refresh,
+    and the bound is 2e-3;
+  - reference order (Jester-shaped): the FP32 oracle's RMSE to 1e-12.
+The Netflix-shaped workload runs in test_fullsize_gpu.py."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from cdmf_gb300 import engine, synth
+
+pytestmark = pytest.mark.gpu
+GOLD = json.load(open(os.path.join(GOLDEN, "workloads.json")))
+FP32_FLOOR = 1e-5
+MIXED_ATOL = 1e-3
+BF16_FIRST_ATOL = 2e-3
+SEQ_ATOL = 1e-12
+
+
+def bit_sum(a):
+    return int(np.ascontiguousarray(a).view(np.uint32).astype(np.int64).sum())
+
+
+def inputs_checksums(R, W0):
+    return dict(m=int(R.m), n=int(R.n), nnz=int(R.nnz), nnz_test=int(R.te_val.size),
+                csr_idx_sum=bit_sum(R.csr_idx), csr_val_sum=bit_sum(R.csr_val), te_row_sum=bit_sum(R.te_row),
+                te_val_sum=bit_sum(R.te_val), w0_sum=bit_sum(W0))
+
+
+@pytest.fixture(scope="module", params=["jester_shape", "ml20m_shape"])
+def workload(request):
+    name = request.param
+    g = GOLD[name]
+    R, run = synth.config(name)
+    assert (run["k"], run["maxiter"], run["maxinneriter"]) == (g["k"], g["maxiter"], g["maxinner"])
+    W0 = synth.initial_w(g["k"], R.m, seed=0)
+    assert inputs_checksums(R, W0) == g["inputs"], "the generator no longer makes the matrix of the trajectories"
+    return name, R, W0, g
+
+
+def _run(R, W0, g, **kw):
+    with engine.Engine(R, g["k"], g["lam"], g["maxiter"], g["maxinner"], **kw) as e:
+        e.set_factors(W0)
+        rm = e.run(g["maxiter"])
+        st = e.stats()
+    assert st["nonfinite"] == 0
+    return np.asarray(rm, np.float64)
+
+
+@pytest.mark.parametrize("version", [1, 3])
+def test_fp32_within_reference_error(workload, version):
+    name, R, W0, g = workload
+    r32, r64 = np.asarray(g["rmse_f32"]), np.asarray(g["rmse_f64"])
+    rm = _run(R, W0, g, residual="f32", version=version)
+    bound = np.maximum(FP32_FLOOR, 2 * np.abs(r32 - r64))
+    assert np.all(np.abs(rm - r64) <= bound), (name, (rm - r64).tolist(), bound.tolist())
+
+
+@pytest.mark.parametrize("residual", ["f16", "bf16"])
+def test_mixed_within_1e3_of_fp64(workload, residual):
+    name, R, W0, g = workload
+    r64 = np.asarray(g["rmse_f64"])
+    rm = _run(R, W0, g, residual=residual)
+    bound = np.full(r64.size, MIXED_ATOL)
+    if residual == "bf16":
+        bound[0] = BF16_FIRST_ATOL
+    assert np.all(np.abs(rm - r64) <= bound), (name, residual, (rm - r64).tolist())
+
+
+def test_reference_order_matches_fp32_oracle(workload):
+    name, R, W0, g = workload
+    if name != "jester_shape":
+        pytest.skip("one thread per line is slow on the 67k-nonzero columns; the Jester shape covers it")
+    rm = _run(R, W0, g, residual="f32", reduce="sequential")
+    assert np.max(np.abs(rm - np.asarray(g["rmse_f32"]))) <= SEQ_ATOL, (rm - np.asarray(g["rmse_f32"])).tolist()
