@@ -101,3 +101,18 @@ def test_oracle_objective_hand_case():
     # rows: nnz 1 and 2; columns: nnz 2 and 1
     assert reg == pytest.approx(0.5 * (1 * 0.25 + 2 * 4.0 + 2 * 1.0 + 1 * 1.0), abs=1e-15)
     assert tot == pytest.approx(sq + reg, abs=1e-15)
+
+
+def test_workload_fixture_jester_shape():
+    """tests/golden/workloads.json (make_workloads.py) for the Jester-shaped
+    workload: the generator still makes the recorded inputs, and the oracle
+    reproduces the recorded FP32 trajectory exactly (the GPU workload tests
+    compare against these trajectories)."""
+    from golden.make_workloads import checksums
+    from cdmf_gb300 import synth
+    g = json.load(open(os.path.join(GOLDEN, "workloads.json")))["jester_shape"]
+    R, run = synth.config("jester_shape")
+    W0 = synth.initial_w(g["k"], R.m, seed=0)
+    assert checksums(R, W0) == g["inputs"]
+    out = oracle.ccdpp(R, W0, g["k"], g["lam"], g["maxiter"], g["maxinner"], threads=4)
+    assert out["rmse"].tolist() == g["rmse_f32"]
