@@ -2,7 +2,8 @@
  * cdmf_synth.h -- seeded synthetic rating matrices in cdmf's in-memory layout.
  *
  * Replaces the reference's unseeded data generators and COO->CSR/CSC
- * converters (data/{a,b,c}/*.py, data/* /*_compress.py:130-155).  The output
+ * converters (the data/a, data/b, data/c generator scripts and the
+ * *_compress.py converters, data/a/a_compress.py:130-155).  The output
  * is the structure the reference's loader fills (src/pmf_util.h:18-36,
  * 121-144): CSR and CSC of the training matrix with 32-bit unsigned indices
  * and float32 values, row indices ascending inside each CSC column and
