@@ -17,17 +17,26 @@
 
 #include <mutex>
 #include <set>
+#include <utility>
 
 namespace cdmf {
 
+// Function attributes belong to the device they were set on, so the
+// launchers set them once per (device, kernel).
+inline std::pair<int, const void*> attr_key(const void* kernel) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return {dev, kernel};
+}
+
 // The sweeps use almost no shared memory; give the unified L1/shared
-// storage to L1, which holds the gather tables.  Once per kernel.
+// storage to L1, which holds the gather tables.
 template <class K>
 void prefer_l1(K kernel) {
     static std::mutex mu;
-    static std::set<const void*> done;
+    static std::set<std::pair<int, const void*>> done;
     std::lock_guard<std::mutex> lk(mu);
-    if (done.insert((const void*)kernel).second)
+    if (done.insert(attr_key((const void*)kernel)).second)
         cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
 }
 
@@ -36,9 +45,9 @@ void prefer_l1(K kernel) {
 template <class K>
 void allow_smem(K kernel, size_t bytes) {
     static std::mutex mu;
-    static std::set<const void*> done;
+    static std::set<std::pair<int, const void*>> done;
     std::lock_guard<std::mutex> lk(mu);
-    if (done.insert((const void*)kernel).second) {
+    if (done.insert(attr_key((const void*)kernel)).second) {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
         cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     }
