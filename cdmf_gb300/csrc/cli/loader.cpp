@@ -11,7 +11,26 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <filesystem>
 #include <iostream>
+#include <new>
+#include <system_error>
+
+// Whether `path` holds at least `bytes` bytes (the reference's fread needs no
+// more); checked for every binary before any array is sized from the meta.
+static bool file_holds(const std::string& path, unsigned long long bytes) {
+    std::error_code ec;
+    const auto have = std::filesystem::file_size(path, ec);
+    if (ec) {
+        fprintf(stderr, "Can't open %s\n", path.c_str());
+        return false;
+    }
+    if (have < bytes) {
+        fprintf(stderr, "FREAD: %s holds %llu bytes, needs %llu\n", path.c_str(), (unsigned long long)have, bytes);
+        return false;
+    }
+    return true;
+}
 
 static bool read_exact(const std::string& path, void* dst, size_t bytes) {
     FILE* f = fopen(path.c_str(), "rb");
@@ -49,20 +68,38 @@ bool load(const char* srcdir, SparseMatrix& R, TestData& T) {
     ok = ok && fscanf(fp, "%lu", &nnz_test) == 1;
     for (int q = 0; ok && q < 3; ++q) ok = fscanf(fp, "%1023s", tbuf[q]) == 1;
     fclose(fp);
-    if (!ok || m < 0 || n < 0) {
+    // the arrays hold 32-bit unsigned indices and pointers (src/pmf_util.h:110-113)
+    const unsigned long kMax = 0xFFFFFFFFul;
+    if (!ok || m < 0 || n < 0 || (unsigned long)m >= kMax || (unsigned long)n >= kMax || nnz > kMax ||
+        nnz_test > kMax) {
         fprintf(stderr, "malformed meta_modified_all\n");
         return false;
     }
+    const unsigned long long b_m = 4ull * (m + 1), b_n = 4ull * (n + 1), b_nnz = 4ull * nnz, b_t = 4ull * nnz_test;
+    if (!file_holds(dir + "/" + buf[3], b_m) || !file_holds(dir + "/" + buf[4], b_nnz) ||
+        !file_holds(dir + "/" + buf[5], b_nnz) || !file_holds(dir + "/" + buf[6], b_n) ||
+        !file_holds(dir + "/" + buf[7], b_nnz) || !file_holds(dir + "/" + buf[8], b_nnz) ||
+        !file_holds(dir + "/" + tbuf[0], b_t) || !file_holds(dir + "/" + tbuf[1], b_t) ||
+        !file_holds(dir + "/" + tbuf[2], b_t))
+        return false;
     auto t2 = std::chrono::high_resolution_clock::now();
     R.rows = m;
     R.cols = n;
     R.nnz = nnz;
-    R.csr_row_ptr.resize(m + 1);
-    R.csr_col_indx.resize(nnz);
-    R.csr_val.resize(nnz);
-    R.csc_col_ptr.resize(n + 1);
-    R.csc_row_indx.resize(nnz);
-    R.csc_val.resize(nnz);
+    try {
+        R.csr_row_ptr.resize(m + 1);
+        R.csr_col_indx.resize(nnz);
+        R.csr_val.resize(nnz);
+        R.csc_col_ptr.resize(n + 1);
+        R.csc_row_indx.resize(nnz);
+        R.csc_val.resize(nnz);
+        T.test_row.resize(nnz_test);
+        T.test_col.resize(nnz_test);
+        T.test_val.resize(nnz_test);
+    } catch (const std::bad_alloc&) {
+        fprintf(stderr, "out of host memory for a %ld x %ld matrix with %lu + %lu entries\n", m, n, nnz, nnz_test);
+        return false;
+    }
     // names 3..8: csr indptr/indices/data, csc indptr/indices/data (src/tools.cpp:318-320)
     if (!read_exact(dir + "/" + buf[3], R.csr_row_ptr.data(), 4 * (m + 1)) ||
         !read_exact(dir + "/" + buf[4], R.csr_col_indx.data(), 4 * nnz) ||
@@ -79,9 +116,6 @@ bool load(const char* srcdir, SparseMatrix& R, TestData& T) {
     T.rows = m;
     T.cols = n;
     T.nnz = nnz_test;
-    T.test_row.resize(nnz_test);
-    T.test_col.resize(nnz_test);
-    T.test_val.resize(nnz_test);
     if (!read_exact(dir + "/" + tbuf[0], T.test_val.data(), 4 * nnz_test) ||
         !read_exact(dir + "/" + tbuf[1], T.test_row.data(), 4 * nnz_test) ||
         !read_exact(dir + "/" + tbuf[2], T.test_col.data(), 4 * nnz_test))
@@ -206,7 +240,12 @@ bool calculate_rmse(const MatData& W, const MatData& H, const char* srcdir, unsi
     bool ok = fscanf(fp, "%u %u", &m, &n) == 2 && fscanf(fp, "%u %1023s", &nnz, buf_train) == 2 &&
               fscanf(fp, "%u %1023s", &nnz_test, buf_test) == 2;
     fclose(fp);
-    if (!ok) return false;
+    if (!ok || k > W.size() || k > H.size()) return false;
+    for (unsigned t = 0; t < k; ++t)
+        if (W[t].size() < m || H[t].size() < n) {
+            fprintf(stderr, "meta: %u x %u, but the factors cover %zu x %zu\n", m, n, W[t].size(), H[t].size());
+            return false;
+        }
     FILE* tf = fopen((dir + "/" + buf_test).c_str(), "r");
     if (!tf) {
         printf("Can't open test file.\n");
