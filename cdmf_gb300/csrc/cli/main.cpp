@@ -72,6 +72,9 @@ int cdmf_cuda(SparseMatrix& R, MatData& W, MatData& H, TestData& T, parameter& p
     }
     std::chrono::duration<double> d = t2 - t1;
     printf("[INFO] OCL Training time: %lf s\n", d.count());
+    // throughput of the whole call (upload, create, outer iterations, download)
+    printf("[INFO] Rank-one updates/s: %.1f, outer iterations/s: %.2f (whole call)\n",
+           (double)k * param.maxiter / d.count(), (double)param.maxiter / d.count());
     for (unsigned t = 0; t < k; ++t) {
         for (long i = 0; i < R.rows; ++i) W[t][i] = Wf[(size_t)t * R.rows + i];
         for (long j = 0; j < R.cols; ++j) H[t][j] = Hf[(size_t)t * R.cols + j];

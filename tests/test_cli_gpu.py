@@ -35,6 +35,7 @@ def test_simple_tree_then_reference_order(tmp_path):
     assert np.max(np.abs(seq - z["rmse"])) <= 1e-6, (seq, z["rmse"])
     assert np.max(np.abs(tree - z["rmse"])) <= 1e-5, (tree, z["rmse"])
     assert out.count("Check... PASS!") == 2, out
+    assert len(re.findall(r"\[INFO\] Rank-one updates/s: [0-9.]+, outer iterations/s: [0-9.]+", out)) == 2, out
     m = re.search(r"\[INFO\] Test RMSE = ([0-9.]+)", out)
     assert m and abs(float(m.group(1)) - z["rmse"][-1]) <= 1e-5, out
 
