@@ -256,6 +256,12 @@ class Batch:
     def __exit__(self, *a):
         self.close()
 
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
     def _check(self, st, where):
         if st != 0:
             msg = self.lib.cdmf_cuda_batch_last_error(self.h)
