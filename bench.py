@@ -28,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -83,9 +84,12 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples: CDMF_CLOCKS_DIR when set (to keep them), else the temp directory
+        folder = os.environ.get("CDMF_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(folder, f"cdmf_clocks_{os.getpid()}_{device}.csv")
 
     def __enter__(self):
+        self.f = None
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
@@ -94,6 +98,9 @@ class ClockSampler:
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            if self.f:
+                self.f.close()
+                os.remove(self.path)
         return self
 
     def __exit__(self, *a):
