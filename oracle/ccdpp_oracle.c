@@ -3,9 +3,9 @@
  *
  * This file restates, in plain C, the algorithm of the reference's OpenMP
  * engine `cdmf_ref` (src/cdmf_ref.cpp) and of its test-RMSE helper
- * `calculate_rmse_directly` (src/tools.cpp:543-582).  It is the checker the
- * parity tests, `__graft_entry__.smoke()` and the `cpu_baseline` leg of
- * `bench.py` compare the CUDA engine against.  Nothing in the product
+ * `calculate_rmse_directly` (src/tools.cpp:543-582).  The parity tests,
+ * `__graft_entry__.smoke()` and the `cpu_baseline` leg of `bench.py` compare
+ * the CUDA engine against it.  Nothing in the product
  * (the `cdmf_gb300` package, `libcdmf_cuda.so`, the `cdmf` CLI) links or
  * calls it.
  *
