@@ -1,0 +1,42 @@
+"""Error of the engine's 16-bit residual mode, modelled on the CPU
+(oracle/mixed_model.c), against the FP64 oracle trajectory of a
+benchmark-shaped workload (tests/golden/workloads.json).  Test and analysis
+infrastructure only.
+
+Usage: python oracle/mixed_model_report.py WORKLOAD STORAGE:REFRESH_EVERY ...
+e.g.   python oracle/mixed_model_report.py ml20m_shape bf16:0 bf16:32 f16:0 f32:0
+prints, per variant, |RMSE - FP64 RMSE| in the first outer iteration and the
+largest over the later ones (and the distance to the FP32 oracle, which is 0
+for f32 storage: the model is then the reference's arithmetic).
+"""
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+from cdmf_gb300 import synth  # noqa: E402
+from oracle import oracle  # noqa: E402
+
+
+def main(name, variants):
+    g = json.load(open(os.path.join(os.path.dirname(HERE), "tests", "golden", "workloads.json")))[name]
+    R, _ = synth.config(name)
+    W0 = synth.initial_w(g["k"], R.m, seed=0)
+    r32, r64 = np.array(g["rmse_f32"]), np.array(g["rmse_f64"])
+    for v in variants:
+        storage, every = v.split(":")
+        t0 = time.time()
+        out = oracle.mixed_model(R, W0, g["k"], g["lam"], g["maxiter"], g["maxinner"], storage=storage,
+                                 refresh_every=int(every))
+        d = out["rmse"] - r64
+        later = np.abs(d[1:]).max() if d.size > 1 else 0.0
+        print(f"{name} {storage} refresh_every={every}: iteration 1 {d[0]:+.2e}, later max {later:.2e}, "
+              f"max vs FP32 oracle {np.abs(out['rmse'] - r32).max():.2e} ({time.time() - t0:.0f} s)", flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1], sys.argv[2:])

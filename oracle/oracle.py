@@ -1,7 +1,8 @@
 """ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
 liboracle_f32.so / liboracle_f64.so: the C restatement of the reference's
-CCD++ engine (oracle/ccdpp_oracle.c).  _ref/libcdmf_ref.so: the reference's
+CCD++ engine (oracle/ccdpp_oracle.c).  libmixed_model.so: a model of the
+engine's 16-bit residual mode (oracle/mixed_model.c).  _ref/libcdmf_ref.so: the reference's
 own src/cdmf_ref.cpp + src/tools.cpp (oracle/build_ref.sh), present only
 where the reference sources are.  Only tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg use this module.
@@ -121,6 +122,38 @@ def objective(R, W, H, res, lam):
     lam = float(np.float32(lam))   # parameter.lambda is a VALUE_TYPE float (src/pmf.h:16)
     reg = lam * (float(np.dot(nr, (W64 * W64).sum(axis=0))) + float(np.dot(nc, (H64 * H64).sum(axis=0))))
     return sq, reg, sq + reg
+
+
+_MODEL = []
+STORAGE = {"f32": 0, "bf16": 1, "f16": 2}
+
+
+def mixed_model(R, W0, k, lam, maxiter, maxinner, storage="bf16", refresh_every=0, threads=0):
+    """CPU model of the engine's 16-bit residual mode (oracle/mixed_model.c):
+    the residual rounded to `storage` on every write, the subtract and the
+    add-back fused, a refresh from FP32 at the start of every outer iteration
+    after the first, and, with refresh_every > 0, every refresh_every features
+    of the first.  With storage "f32" it is the reference's arithmetic.
+    Returns dict(W, H, rmse)."""
+    if not _MODEL:
+        path = os.path.join(HERE, "libmixed_model.so")
+        if not os.path.exists(path):
+            build()
+        lib = ctypes.CDLL(path)
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        lib.mixed_model_ccdpp.argtypes = [ctypes.POINTER(OracleProblem), ctypes.c_uint32, ctypes.c_double, i, i, i, i,
+                                          i, vp, vp, vp]
+        lib.mixed_model_ccdpp.restype = i
+        _MODEL.append(lib)
+    P = problem(R)
+    W = np.ascontiguousarray(W0, np.float32).copy()
+    H = np.zeros((k, R.n), np.float32)
+    rm = np.zeros(max(1, maxiter), np.float64)
+    st = _MODEL[0].mixed_model_ccdpp(ctypes.byref(P), k, lam, maxiter, maxinner, STORAGE[storage], refresh_every,
+                                     threads, _p(W), _p(H), _p(rm))
+    if st != 0:
+        raise RuntimeError("mixed_model_ccdpp failed (CSC not the transpose of CSR, or out of memory)")
+    return dict(W=W, H=H, rmse=rm[:maxiter])
 
 
 def reference_available():

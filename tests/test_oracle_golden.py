@@ -116,3 +116,36 @@ def test_workload_fixture_jester_shape():
     assert checksums(R, W0) == g["inputs"]
     out = oracle.ccdpp(R, W0, g["k"], g["lam"], g["maxiter"], g["maxinner"], threads=4)
     assert out["rmse"].tolist() == g["rmse_f32"]
+
+
+@pytest.mark.parametrize("name", ["simple", "tricky_simple", "mini"])
+def test_mixed_model_with_fp32_storage_is_the_reference(name):
+    """oracle/mixed_model.c with FP32 storage (fused subtract and add-back,
+    one residual array) reproduces the reference's own outputs bit for bit."""
+    R, z = load_golden(name)
+    md = META[name]
+    out = oracle.mixed_model(R, z["W0"], md["k"], md["lam"], md["maxiter"], md["maxinner"], storage="f32",
+                             threads=2)
+    assert np.array_equal(bits(out["W"]), bits(z["W_hist"][-1]))
+    assert np.array_equal(bits(out["H"]), bits(z["H_hist"][-1]))
+    assert np.array_equal(out["rmse"], z["rmse"])
+
+
+def test_mixed_model_first_iteration_drift_jester_shape():
+    """The 16-bit model on the Jester-shaped workload: every outer iteration
+    within 1e-3 of the FP64 oracle; the first outer iteration, which runs
+    before the first refresh, drifts more in BF16 than in FP16, and less when
+    refreshes are added inside it."""
+    from cdmf_gb300 import synth
+    g = json.load(open(os.path.join(GOLDEN, "workloads.json")))["jester_shape"]
+    R, _ = synth.config("jester_shape")
+    W0 = synth.initial_w(g["k"], R.m, seed=0)
+    r64 = np.array(g["rmse_f64"])
+    err = {}
+    for storage, every in (("bf16", 0), ("bf16", 4), ("f16", 0)):
+        out = oracle.mixed_model(R, W0, g["k"], g["lam"], g["maxiter"], g["maxinner"], storage=storage,
+                                 refresh_every=every)
+        d = np.abs(out["rmse"] - r64)
+        assert np.all(d <= 1e-3), (storage, every, d.tolist())
+        err[(storage, every)] = d[0]
+    assert err[("f16", 0)] < err[("bf16", 0)] and err[("bf16", 4)] < err[("bf16", 0)], err
