@@ -7,7 +7,8 @@ Usage: python oracle/mixed_model_report.py WORKLOAD STORAGE:REFRESH_EVERY ...
 e.g.   python oracle/mixed_model_report.py ml20m_shape bf16:0 bf16:32 f16:0 f32:0
 prints, per variant, |RMSE - FP64 RMSE| in the first outer iteration and the
 largest over the later ones (and the distance to the FP32 oracle, which is 0
-for f32 storage: the model is then the reference's arithmetic).
+for f32 storage: the model is then the reference's arithmetic), then
+RMSE - FP64 RMSE after every outer iteration.
 """
 import json
 import os
@@ -36,6 +37,7 @@ def main(name, variants):
         later = np.abs(d[1:]).max() if d.size > 1 else 0.0
         print(f"{name} {storage} refresh_every={every}: iteration 1 {d[0]:+.2e}, later max {later:.2e}, "
               f"max vs FP32 oracle {np.abs(out['rmse'] - r32).max():.2e} ({time.time() - t0:.0f} s)", flush=True)
+        print("  per outer iteration: " + " ".join(f"{x:+.1e}" for x in d), flush=True)
 
 
 if __name__ == "__main__":
