@@ -9,6 +9,10 @@ prints, per variant, |RMSE - FP64 RMSE| in the first outer iteration and the
 largest over the later ones (and the distance to the FP32 oracle, which is 0
 for f32 storage: the model is then the reference's arithmetic), then
 RMSE - FP64 RMSE after every outer iteration.
+
+WORKLOAD batch64 runs the 64 uneven problems of the batched benchmark
+(synth.batch_specs, W0 seeded by problem), the FP64 oracle computed on the
+spot, and prints per variant the problems furthest from FP64.
 """
 import json
 import os
@@ -40,5 +44,34 @@ def main(name, variants):
         print("  per outer iteration: " + " ".join(f"{x:+.1e}" for x in d), flush=True)
 
 
+def main_batch(variants, count=64):
+    specs = synth.batch_specs(count, seed=0)
+    probs = []
+    for q, sp in enumerate(specs):
+        R = synth.generate(**sp["matrix"])
+        run = sp["run"]
+        W0 = synth.initial_w(run["k"], R.m, seed=q)
+        r64 = oracle.ccdpp(R, W0.astype(np.float64), run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"],
+                           dtype=np.float64)["rmse"]
+        probs.append((R, run, W0, r64))
+    for v in variants:
+        storage, every = v.split(":")
+        worst = []
+        for q, (R, run, W0, r64) in enumerate(probs):
+            out = oracle.mixed_model(R, W0, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"],
+                                     storage=storage, refresh_every=int(every))
+            d = np.abs(out["rmse"] - r64)
+            worst.append((float(d.max()), int(d.argmax()) + 1, q, run["k"], run["lambda_"], int(R.nnz)))
+        worst.sort(reverse=True)
+        over = sum(1 for w in worst if w[0] > 1e-3)
+        print(f"batch64 {storage} refresh_every={every}: {over} of {len(worst)} problems beyond 1e-3 of FP64; "
+              f"largest {worst[0][0]:.2e}", flush=True)
+        for w in worst[:5]:
+            print(f"  {w[0]:.2e} at outer iteration {w[1]}: problem {w[2]}, k={w[3]}, lambda={w[4]}, nnz={w[5]}")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1], sys.argv[2:])
+    if sys.argv[1] == "batch64":
+        main_batch(sys.argv[2:])
+    else:
+        main(sys.argv[1], sys.argv[2:])
