@@ -13,18 +13,25 @@ by make_golden.py; these trajectories are its output on larger inputs, too
 slow to recompute inside a GPU test (netflix_shape takes tens of minutes of
 CPU per precision).
 
-Usage: python tests/golden/make_workloads.py [workload ...]   (merges into the file)
+Where the reference's sources are (oracle/_ref built by oracle/build_ref.sh),
+`--pin` runs the reference's own engine on a workload already in the file and
+checks the oracle against it bit for bit (final W and H, last RMSE) before
+marking the entry "reference_pinned".
+
+Usage: python tests/golden/make_workloads.py [workload ...]        (merges into the file)
+       python tests/golden/make_workloads.py --pin [workload ...]  (pins existing entries)
 """
 import json
 import os
 import sys
+import tempfile
 import time
 
 import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
-from cdmf_gb300 import synth  # noqa: E402
+from cdmf_gb300 import formats, synth  # noqa: E402
 from oracle import oracle  # noqa: E402
 
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "workloads.json")
@@ -56,6 +63,29 @@ def make(name):
     return out
 
 
+def pin(name, entry):
+    """The reference's cdmf_ref on the workload against the oracle, bit for bit."""
+    if not oracle.reference_available():
+        raise SystemExit("oracle/_ref is not built (oracle/build_ref.sh needs the reference sources)")
+    R, run = synth.config(name)
+    k, lam, T, it = entry["k"], entry["lam"], entry["maxinner"], entry["maxiter"]
+    W0 = synth.initial_w(k, R.m, seed=0)
+    if checksums(R, W0) != entry["inputs"]:
+        raise SystemExit(f"{name}: the generator no longer makes the recorded inputs")
+    t0 = time.time()
+    with tempfile.TemporaryDirectory(dir=os.path.dirname(OUT)) as tmp:
+        formats.write_dir(tmp, R)
+        ref = oracle.reference_run(tmp, W0, k, lam, it, T, threads=os.cpu_count() or 1)
+    o = oracle.ccdpp(R, W0, k, lam, it, T)
+    same = (np.array_equal(o["W"].view(np.uint32), ref["W"].view(np.uint32))
+            and np.array_equal(o["H"].view(np.uint32), ref["H"].view(np.uint32))
+            and ref["rmse"] == o["rmse"][-1] == entry["rmse_f32"][-1])
+    if not same:
+        raise SystemExit(f"{name}: the oracle differs from the reference; nothing written")
+    print(f"{name}: oracle == reference bit for bit ({time.time() - t0:.0f} s)", flush=True)
+    entry["reference_pinned"] = True
+
+
 def main(names):
     data = json.load(open(OUT)) if os.path.exists(OUT) else {}
     for name in names:
@@ -65,5 +95,17 @@ def main(names):
             f.write("\n")
 
 
+def main_pin(names):
+    data = json.load(open(OUT))
+    for name in names:
+        pin(name, data[name])
+        with open(OUT, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+            f.write("\n")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1:] or DEFAULT)
+    if sys.argv[1:2] == ["--pin"]:
+        main_pin(sys.argv[2:] or ("jester_shape", "ml20m_shape"))
+    else:
+        main(sys.argv[1:] or DEFAULT)
