@@ -112,7 +112,7 @@ def test_workload_fixture_jester_shape():
     from cdmf_gb300 import synth
     gold = json.load(open(os.path.join(GOLDEN, "workloads.json")))
     # make_workloads.py --pin ran the reference's own engine on these
-    assert gold["jester_shape"].get("reference_pinned") and gold["ml20m_shape"].get("reference_pinned")
+    assert all(gold[w].get("reference_pinned") for w in ("jester_shape", "ml20m_shape", "netflix_shape"))
     g = gold["jester_shape"]
     R, run = synth.config("jester_shape")
     W0 = synth.initial_w(g["k"], R.m, seed=0)
