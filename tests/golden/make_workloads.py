@@ -9,9 +9,9 @@ Workloads (cdmf_gb300.synth presets, W0 = synth.initial_w(k, m, seed=0), H = 0):
   ml20m_shape    138,493 x 26,744, 19.6M nonzeros, k=128, lambda=0.1, 10 x 3
   netflix_shape  480,189 x 17,770, 99.1M nonzeros, k=64, lambda=0.05, 20 x 1
 The oracle restatement is pinned bit for bit to the reference's own engine
-by make_golden.py; these trajectories are its output on larger inputs, too
-slow to recompute inside a GPU test (netflix_shape takes tens of minutes of
-CPU per precision).
+by make_golden.py on small cases and by `--pin` below on these workloads;
+the trajectories are too slow to recompute inside a GPU test (netflix_shape
+takes minutes of CPU per precision).
 
 Where the reference's sources are (oracle/_ref built by oracle/build_ref.sh),
 `--pin` runs the reference's own engine on a workload already in the file and
