@@ -10,6 +10,7 @@ Directory layout, as the reference's converters write it
 Indices are int32 (read as 32-bit unsigned), values float32.
 """
 import os
+import warnings
 from dataclasses import dataclass
 
 import numpy as np
@@ -126,7 +127,9 @@ def from_coo(m, n, rows, cols, vals, te_rows, te_cols, te_vals):
 
 def read_text_ratings(path):
     """1-based "u<ws>i<ws>r" lines -> 0-based int arrays and float values."""
-    data = np.loadtxt(path, dtype=np.float64, ndmin=2)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", UserWarning)   # an empty file is an empty set here
+        data = np.loadtxt(path, dtype=np.float64, ndmin=2)
     if data.size == 0:
         return np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros(0, np.float64)
     return data[:, 0].astype(np.int64) - 1, data[:, 1].astype(np.int64) - 1, data[:, 2]

@@ -86,3 +86,29 @@ def test_initial_col_matches_reference():
     _, z = load_golden("simple")
     X = synth.reference_initial_col(10, 6)
     assert np.array_equal(X.view(np.uint32), z["W0"].view(np.uint32))
+
+
+def test_text_pair_and_test_file(tmp_path):
+    """The reference fixtures' 1-based text format: a train/test pair read
+    with from_text gives the structures from_coo gives for the 0-based
+    entries, and the test.txt that write_dir emits for -p 1 reads back to
+    the same test set."""
+    R, _ = load_golden("mini")
+    rows, cols, vals = R.coo()
+    train = tmp_path / "mini.dat"
+    test = tmp_path / "mini.test"
+    train.write_text("".join(f"{i + 1} {j + 1} {float(v)!r}\n" for i, j, v in zip(rows, cols, vals)))
+    test.write_text("".join(f"{i + 1}\t{j + 1}\t{float(v)!r}\n" for i, j, v in zip(R.te_row, R.te_col, R.te_val)))
+    S = formats.from_text(str(train), str(test), R.m, R.n)
+    for f in ("csr_ptr", "csr_idx", "csc_ptr", "csc_idx", "te_row", "te_col"):
+        assert np.array_equal(getattr(S, f), getattr(R, f)), f
+    for f in ("csr_val", "csc_val", "te_val"):
+        assert np.array_equal(getattr(S, f).view(np.uint32), getattr(R, f).view(np.uint32)), f
+    d = tmp_path / "dir"
+    formats.write_dir(str(d), R)
+    tr, tc, tv = formats.read_text_ratings(str(d / "test.txt"))
+    assert np.array_equal(tr, R.te_row) and np.array_equal(tc, R.te_col)
+    assert np.array_equal(tv.astype(np.float32).view(np.uint32), R.te_val.view(np.uint32))
+    empty = tmp_path / "empty.txt"
+    empty.write_text("")
+    assert all(a.size == 0 for a in formats.read_text_ratings(str(empty)))
