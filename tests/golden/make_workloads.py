@@ -18,8 +18,12 @@ Where the reference's sources are (oracle/_ref built by oracle/build_ref.sh),
 checks the oracle against it bit for bit (final W and H, last RMSE) before
 marking the entry "reference_pinned".
 
-Usage: python tests/golden/make_workloads.py [workload ...]        (merges into the file)
-       python tests/golden/make_workloads.py --pin [workload ...]  (pins existing entries)
+`--model` adds the trajectories of the CPU model of the engine's 16-bit
+residual mode (oracle/mixed_model.c) for BF16 and FP16 storage.
+
+Usage: python tests/golden/make_workloads.py [workload ...]          (merges into the file)
+       python tests/golden/make_workloads.py --pin [workload ...]    (pins existing entries)
+       python tests/golden/make_workloads.py --model [workload ...]  (adds the 16-bit model)
 """
 import json
 import os
@@ -95,6 +99,30 @@ def main(names):
             f.write("\n")
 
 
+def model(name, entry):
+    """The 16-bit model's trajectories (oracle/mixed_model.c, the engine's
+    refresh schedule) for BF16 and FP16 storage."""
+    R, _ = synth.config(name)
+    W0 = synth.initial_w(entry["k"], R.m, seed=0)
+    if checksums(R, W0) != entry["inputs"]:
+        raise SystemExit(f"{name}: the generator no longer makes the recorded inputs")
+    for storage in ("bf16", "f16"):
+        t0 = time.time()
+        out = oracle.mixed_model(R, W0, entry["k"], entry["lam"], entry["maxiter"], entry["maxinner"],
+                                 storage=storage)
+        entry["model_" + storage] = [float(x) for x in out["rmse"]]
+        print(f"{name} model {storage}: {time.time() - t0:.0f} s", flush=True)
+
+
+def main_model(names):
+    data = json.load(open(OUT))
+    for name in names:
+        model(name, data[name])
+        with open(OUT, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+            f.write("\n")
+
+
 def main_pin(names):
     data = json.load(open(OUT))
     for name in names:
@@ -107,5 +135,7 @@ def main_pin(names):
 if __name__ == "__main__":
     if sys.argv[1:2] == ["--pin"]:
         main_pin(sys.argv[2:] or ("jester_shape", "ml20m_shape"))
+    elif sys.argv[1:2] == ["--model"]:
+        main_model(sys.argv[2:] or ("jester_shape", "ml20m_shape"))
     else:
         main(sys.argv[1:] or DEFAULT)

@@ -151,4 +151,6 @@ def test_mixed_model_first_iteration_drift_jester_shape():
         d = np.abs(out["rmse"] - r64)
         assert np.all(d <= 1e-3), (storage, every, d.tolist())
         err[(storage, every)] = d[0]
+        if every == 0:   # the trajectories the GPU workload test compares against
+            assert out["rmse"].tolist() == g["model_" + storage]
     assert err[("f16", 0)] < err[("bf16", 0)] and err[("bf16", 4)] < err[("bf16", 0)], err

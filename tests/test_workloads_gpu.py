@@ -10,6 +10,8 @@ same algorithm in double), after every outer iteration:
     run (outer iteration 2 on); in outer iteration 1 the residual has gone
     through k (k = 128 here) rank-one updates stored in BF16 with no refresh,
     and the bound is 2e-3;
+  - FP16 and BF16: on the trajectory of the CPU model of the 16-bit mode
+    (oracle/mixed_model.c) to within twice the reference's FP32 error + 2e-5;
   - reference order (Jester-shaped): the FP32 oracle's RMSE to 1e-12.
 The Netflix-shaped workload runs in test_fullsize_gpu.py."""
 import json
@@ -27,6 +29,7 @@ FP32_FLOOR = 1e-5
 MIXED_ATOL = 1e-3
 BF16_FIRST_ATOL = 2e-3
 SEQ_ATOL = 1e-12
+MODEL_ATOL = 2e-5
 
 
 def bit_sum(a):
@@ -77,6 +80,12 @@ def test_mixed_within_1e3_of_fp64(workload, residual):
     if residual == "bf16":
         bound[0] = BF16_FIRST_ATOL
     assert np.all(np.abs(rm - r64) <= bound), (name, residual, (rm - r64).tolist())
+    # the engine follows the CPU model of its 16-bit mode (oracle/mixed_model.c)
+    # to within twice the reference's own FP32 error: the model sums each
+    # line sequentially, as the reference does, the engine in trees
+    model, r32 = np.asarray(g["model_" + residual]), np.asarray(g["rmse_f32"])
+    tol = 2 * np.abs(r32 - r64) + MODEL_ATOL
+    assert np.all(np.abs(rm - model) <= tol), (name, residual, (rm - model).tolist(), tol.tolist())
 
 
 def test_reference_order_matches_fp32_oracle(workload):
