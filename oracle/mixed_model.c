@@ -56,9 +56,33 @@ static float store_bf16(float x) {
     return x;
 }
 
+/* The binary16 value nearest to x (ties to even), as a float: 10 mantissa
+ * bits for normal results, multiples of 2^-24 below 2^-14, infinity from
+ * 65520 up.  Written out rather than through a compiler half type so that it
+ * builds the same everywhere. */
+static float store_f16(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    const uint32_t sign = u & 0x80000000u, a = u & 0x7fffffffu;
+    if (a >= 0x7f800000u) return x;                                  /* Inf, NaN */
+    if (a >= 0x477ff000u) {                                          /* >= 65520 */
+        u = sign | 0x7f800000u;
+        memcpy(&x, &u, 4);
+        return x;
+    }
+    if (a < 0x38800000u) {                                           /* < 2^-14: subnormal */
+        const float q = nearbyintf(fabsf(x) * 0x1p24f) * 0x1p-24f;
+        return sign ? -q : q;
+    }
+    uint32_t r = (a + 0xfffu + ((a >> 13) & 1u)) & ~0x1fffu;        /* drop 13 of 23 bits */
+    r |= sign;
+    memcpy(&x, &r, 4);
+    return x;
+}
+
 static float store(float x, int storage) {
     if (storage == 1) return store_bf16(x);
-    if (storage == 2) return (float)(_Float16)x;        /* IEEE binary16, round to nearest even */
+    if (storage == 2) return store_f16(x);
     return x;
 }
 
