@@ -14,8 +14,9 @@
  *     is recomputed from the FP32 ratings and factors (r = store(R - W.H),
  *     the dot product in t order with fmaf), as the engine's refresh does;
  *   - refresh_every > 0 adds the same refresh every refresh_every features
- *     of the first outer iteration (a schedule the engine does not run; the
- *     model measures what it would buy).
+ *     of the first outer iteration, or of every outer iteration with
+ *     refresh_all (schedules the engine does not run; the model measures
+ *     what they would buy).
  * Line sums are sequential in index order with separate roundings, as in the
  * reference (src/cdmf_ref.cpp:7-17), so with FP32 storage the model is the
  * reference's arithmetic and reproduces oracle/ccdpp_oracle.c bit for bit
@@ -110,10 +111,11 @@ static double test_rmse(const model_problem *P, uint32_t k, const float *W, cons
 }
 
 /* W (k x m) in/out, H (k x n) out (zeroed first), rmse[maxiter].  storage:
- * 0 = FP32, 1 = BF16, 2 = FP16.  Returns 0, or -1 when the CSC arrays are not
+ * 0 = FP32, 1 = BF16, 2 = FP16; refresh_every / refresh_all: the extra
+ * refreshes above (0 / 0: the engine's schedule).  Returns 0, or -1 when the CSC arrays are not
  * the canonical transpose of the CSR arrays or memory runs out. */
 int mixed_model_ccdpp(const model_problem *P, uint32_t k, double lambda_d, int maxiter, int maxinner, int storage,
-                      int refresh_every, int threads, float *W, float *H, double *rmse) {
+                      int refresh_every, int refresh_all, int threads, float *W, float *H, double *rmse) {
     const int64_t m = P->m, n = P->n, N = P->nnz;
     const float lambda = (float)lambda_d;
     if (threads > 0) omp_set_num_threads(threads);
@@ -137,9 +139,13 @@ int mixed_model_ccdpp(const model_problem *P, uint32_t k, double lambda_d, int m
     memset(H, 0, sizeof(float) * (size_t)k * (size_t)n);
     int pending = -1, since_refresh = 0;
     for (int oiter = 1; oiter <= maxiter; ++oiter) {
-        if (oiter > 1 && storage != 0) { refresh(P, storage, k, W, H, r); pending = -1; }
+        if (oiter > 1 && storage != 0) {
+            refresh(P, storage, k, W, H, r);
+            pending = -1;
+            since_refresh = 0;
+        }
         for (uint32_t t = 0; t < k; ++t) {
-            if (oiter == 1 && storage != 0 && refresh_every > 0 && since_refresh >= refresh_every) {
+            if ((oiter == 1 || refresh_all) && storage != 0 && refresh_every > 0 && since_refresh >= refresh_every) {
                 refresh(P, storage, k, W, H, r);
                 pending = -1;
                 since_refresh = 0;

@@ -3,8 +3,9 @@
 benchmark-shaped workload (tests/golden/workloads.json).  Test and analysis
 infrastructure only.
 
-Usage: python oracle/mixed_model_report.py WORKLOAD STORAGE:REFRESH_EVERY ...
+Usage: python oracle/mixed_model_report.py WORKLOAD STORAGE:REFRESH_EVERY[:all] ...
 e.g.   python oracle/mixed_model_report.py ml20m_shape bf16:0 bf16:32 f16:0 f32:0
+(":all" keeps the extra refreshes in every outer iteration, not only the first)
 prints, per variant, |RMSE - FP64 RMSE| in the first outer iteration and the
 largest over the later ones (and the distance to the FP32 oracle, which is 0
 for f32 storage: the model is then the reference's arithmetic), then
@@ -33,10 +34,10 @@ def main(name, variants):
     W0 = synth.initial_w(g["k"], R.m, seed=0)
     r32, r64 = np.array(g["rmse_f32"]), np.array(g["rmse_f64"])
     for v in variants:
-        storage, every = v.split(":")
+        storage, every, *scope = v.split(":")
         t0 = time.time()
         out = oracle.mixed_model(R, W0, g["k"], g["lam"], g["maxiter"], g["maxinner"], storage=storage,
-                                 refresh_every=int(every))
+                                 refresh_every=int(every), refresh_all=scope == ["all"])
         d = out["rmse"] - r64
         later = np.abs(d[1:]).max() if d.size > 1 else 0.0
         print(f"{name} {storage} refresh_every={every}: iteration 1 {d[0]:+.2e}, later max {later:.2e}, "
@@ -55,11 +56,11 @@ def main_batch(variants, count=64):
                            dtype=np.float64)["rmse"]
         probs.append((R, run, W0, r64))
     for v in variants:
-        storage, every = v.split(":")
+        storage, every, *scope = v.split(":")
         worst = []
         for q, (R, run, W0, r64) in enumerate(probs):
             out = oracle.mixed_model(R, W0, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"],
-                                     storage=storage, refresh_every=int(every))
+                                     storage=storage, refresh_every=int(every), refresh_all=scope == ["all"])
             d = np.abs(out["rmse"] - r64)
             worst.append((float(d.max()), int(d.argmax()) + 1, q, run["k"], run["lambda_"], int(R.nnz)))
         worst.sort(reverse=True)

@@ -128,13 +128,13 @@ _MODEL = []
 STORAGE = {"f32": 0, "bf16": 1, "f16": 2}
 
 
-def mixed_model(R, W0, k, lam, maxiter, maxinner, storage="bf16", refresh_every=0, threads=0):
+def mixed_model(R, W0, k, lam, maxiter, maxinner, storage="bf16", refresh_every=0, refresh_all=False, threads=0):
     """CPU model of the engine's 16-bit residual mode (oracle/mixed_model.c):
     the residual rounded to `storage` on every write, the subtract and the
     add-back fused, a refresh from FP32 at the start of every outer iteration
     after the first, and, with refresh_every > 0, every refresh_every features
-    of the first.  With storage "f32" it is the reference's arithmetic.
-    Returns dict(W, H, rmse)."""
+    of the first (of every one with refresh_all).  With storage "f32" it is
+    the reference's arithmetic.  Returns dict(W, H, rmse)."""
     if not _MODEL:
         path = os.path.join(HERE, "libmixed_model.so")
         if not os.path.exists(path):
@@ -142,7 +142,7 @@ def mixed_model(R, W0, k, lam, maxiter, maxinner, storage="bf16", refresh_every=
         lib = ctypes.CDLL(path)
         vp, i = ctypes.c_void_p, ctypes.c_int
         lib.mixed_model_ccdpp.argtypes = [ctypes.POINTER(OracleProblem), ctypes.c_uint32, ctypes.c_double, i, i, i, i,
-                                          i, vp, vp, vp]
+                                          i, i, vp, vp, vp]
         lib.mixed_model_ccdpp.restype = i
         _MODEL.append(lib)
     P = problem(R)
@@ -150,7 +150,7 @@ def mixed_model(R, W0, k, lam, maxiter, maxinner, storage="bf16", refresh_every=
     H = np.zeros((k, R.n), np.float32)
     rm = np.zeros(max(1, maxiter), np.float64)
     st = _MODEL[0].mixed_model_ccdpp(ctypes.byref(P), k, lam, maxiter, maxinner, STORAGE[storage], refresh_every,
-                                     threads, _p(W), _p(H), _p(rm))
+                                     int(bool(refresh_all)), threads, _p(W), _p(H), _p(rm))
     if st != 0:
         raise RuntimeError("mixed_model_ccdpp failed (CSC not the transpose of CSR, or out of memory)")
     return dict(W=W, H=H, rmse=rm[:maxiter])
