@@ -196,3 +196,19 @@ def test_integration_shim_compiles_and_links(tmp_path):
                         "-lcdmf_cuda", "-Wl,-rpath," + os.path.dirname(_build.LIB)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_integration_python_example_parses_and_names_real_functions():
+    """The Python example in INTEGRATION.md is valid Python and calls
+    functions the package has."""
+    import ast
+    from cdmf_gb300 import formats, synth
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = re.findall(r"```python\n(.*?)```", doc, flags=re.S)
+    assert blocks
+    mods = {"engine": engine, "formats": formats, "synth": synth}
+    for b in blocks:
+        tree = ast.parse(b)
+        for node in ast.walk(tree):
+            if isinstance(node, ast.Attribute) and isinstance(node.value, ast.Name) and node.value.id in mods:
+                assert hasattr(mods[node.value.id], node.attr), f"{node.value.id}.{node.attr}"
