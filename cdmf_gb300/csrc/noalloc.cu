@@ -1,20 +1,22 @@
 // Test RMSE without any allocation by the library (cdmf_cuda_rmse_coo_noalloc).
 //
 // Some callers cannot let a library call cudaMalloc: a serving process that
-// owns every device allocation through its own pool, a caller inside a
-// stream capture that must not add allocation nodes, or an embedded runtime
-// whose memory budget is fixed at start-up.  This entry point computes the
-// same test RMSE as cdmf_cuda_rmse_coo, on device arrays the caller already
-// holds, and keeps the kernel's scratch (per-block partial sums, the result
-// slot, the NaN count and the arrival counter) in a fixed file-scope device
-// array instead of allocating it.
+// hands out all of its device memory from its own pool (an allocation made
+// behind the pool's back is not in its accounting, and fails once the pool
+// holds the memory), or an embedded runtime whose memory budget is fixed at
+// start-up.  This entry point computes the same test RMSE as
+// cdmf_cuda_rmse_coo, on device arrays the caller already holds, and keeps
+// the kernel's scratch (per-block partial sums, the result slot, the NaN
+// count and the arrival counter) in a fixed file-scope device array instead
+// of allocating it.
 //
 // The array lives in every device that loads the library, until the process
 // exits.  It is shared by all calls: calls that overlap on the GPU (from
 // several streams or threads at once) race on it and must be serialised by
-// the caller.  Its address is looked up once per device, on the first call
-// made with that device current; make that first call before any stream
-// capture begins.
+// the caller.  Its device address is looked up once per device, on the first
+// call made with that device current, and kept; make that first call before
+// any stream capture begins.  A device reset moves the array, so a caller
+// that resets a device does not call this entry point on it again.
 #include <cdmf_cuda.h>
 
 #include "sweep_kernels.cuh"

@@ -153,20 +153,25 @@ int cdmf_cuda_rmse_coo(uint32_t k, int64_t m, int64_t n, const float* W, const f
                        double* rmse, int64_t* nan_count);
 
 /* Test RMSE on device arrays without any allocation by the library.  It has
- * no counterpart in the reference.  For callers that cannot let a library
- * call cudaMalloc (a process whose device memory all comes from its own pool,
- * work recorded into a stream capture, a runtime with a fixed memory
- * budget): W (k x m), H (k x n), test_row/test_col/test_val (nnz_test) are
- * DEVICE pointers the caller owns, indices 0-based and in range; rmse and
- * nan_count are host pointers.  Same arithmetic and result as
- * cdmf_cuda_rmse_coo.  The kernel's scratch is a fixed file-scope device
- * array of about 5 KB (608 block partials and three counters), held by every
- * device that loads the library until exit and shared by all calls: calls
- * that overlap on the GPU race on it.  The first call on a device looks up
- * the array's address and should come before any stream capture.  Test sets
- * larger than CDMF_NOALLOC_MAX_TEST entries (the reference counts entries in
- * an int) are rejected with CDMF_ERR_TOO_LARGE.  stream: a cudaStream_t, or
- * NULL for the default stream; the call waits for its own work. */
+ * no counterpart in the reference.  It serves callers that cannot let a
+ * library call cudaMalloc: a serving process that hands out every byte of
+ * device memory from its own pool (a library allocation would sit outside
+ * that pool's accounting and can fail once the pool holds the memory), or a
+ * runtime whose device memory budget is fixed when it starts.  W (k x m),
+ * H (k x n), test_row/test_col/test_val (nnz_test) are DEVICE pointers the
+ * caller owns, indices 0-based and in range; rmse and nan_count are host
+ * pointers.  Same arithmetic and result as cdmf_cuda_rmse_coo.  The kernel's
+ * scratch is a fixed file-scope device array of about 5 KB (608 block
+ * partials and three counters), held by every device that loads the library
+ * until exit and shared by all calls: calls that overlap on the GPU race on
+ * it, so the caller serialises them.  The first call on a device looks up the
+ * array's device address and keeps it; make that first call before any
+ * stream capture begins, and do not call again on a device after resetting
+ * it (cudaDeviceReset), which moves the array.  Test sets larger than
+ * CDMF_NOALLOC_MAX_TEST entries (the reference counts entries in an int) are
+ * rejected with CDMF_ERR_TOO_LARGE.  stream: a cudaStream_t, or NULL for the
+ * default stream; the call copies the result to host memory and waits for
+ * its own work before it returns. */
 #define CDMF_NOALLOC_MAX_TEST 2147483647LL
 int cdmf_cuda_rmse_coo_noalloc(uint32_t k, int64_t m, int64_t n, const float* W, const float* H, int64_t nnz_test,
                                const uint32_t* test_row, const uint32_t* test_col, const double* test_val,

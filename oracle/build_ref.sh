@@ -1,13 +1,14 @@
 #!/usr/bin/env bash
 # Builds oracle/_ref/libcdmf_ref.so from the reference's own CPU sources,
-# unmodified, where they lie (default /root/reference; override with
-# CDMF_REFERENCE).  Test infrastructure only; the output stays out of git.
+# unmodified, where they lie: the first argument, else $CDMF_REFERENCE, else
+# a checkout named `reference` beside this repository.  Test infrastructure
+# only; the output stays out of git.
 # Flags follow the reference's CMakeLists.txt:15-17 (-DVALUE_TYPE=float, C++14,
 # OpenMP); -O2 is added and changes no result on x86-64 (no FMA in the
 # baseline ISA, no fast-math).
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${CDMF_REFERENCE:-/root/reference}"
+REF="${1:-${CDMF_REFERENCE:-$HERE/../../reference}}"
 if [ ! -f "$REF/src/cdmf_ref.cpp" ]; then
     echo "build_ref.sh: reference sources not found under $REF; skipping" >&2
     exit 0

@@ -102,7 +102,8 @@ def mini_matrix():
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CDMF_REFERENCE", "/root/reference")
+    ref_root = (sys.argv[1] if len(sys.argv) > 1 else
+                os.environ.get("CDMF_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference")))
     oracle.build()
     if not oracle.reference_available():
         raise SystemExit("oracle/_ref/libcdmf_ref.so missing: the reference sources are needed")

@@ -137,78 +137,19 @@ def test_anonymouslib_header_compiles_and_links(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-# Stand-ins for the reference's host types, with the members the shim uses
-# (src/pmf_util.h: SparseMatrix accessors, MatData, TestData; src/pmf.h:
-# parameter), so the shim can be compiled here without the reference tree.
-_REFERENCE_STANDINS = {
-    "tools.h": """#pragma once
-#include <algorithm>
-#include <cstdio>
-#include <cstdlib>
-#include <vector>
-typedef std::vector<std::vector<float> > MatData;
-struct SparseMatrix {
-    long rows, cols, nnz;
-    unsigned *csr_row_ptr_, *csr_col_indx_, *csc_col_ptr_, *csc_row_indx_;
-    float *csr_val_, *csc_val_;
-    unsigned* get_csr_row_ptr() { return csr_row_ptr_; }
-    unsigned* get_csr_col_indx() { return csr_col_indx_; }
-    float* get_csr_val() { return csr_val_; }
-    unsigned* get_csc_col_ptr() { return csc_col_ptr_; }
-    unsigned* get_csc_row_indx() { return csc_row_indx_; }
-    float* get_csc_val() { return csc_val_; }
-};
-struct TestData {
-    long nnz;
-    unsigned *row, *col;
-    float* val;
-    unsigned* getTestRow() { return row; }
-    unsigned* getTestCol() { return col; }
-    float* getTestVal() { return val; }
-};
-struct parameter {
-    unsigned k;
-    float lambda;
-    int maxiter, maxinneriter, version;
-};
-""",
-    "cdmf.h": "#pragma once\n#include \"tools.h\"\n",
-}
-
-
 def test_integration_shim_compiles_and_links(tmp_path):
-    """The C++ shim that INTEGRATION.md gives a maintainer of the reference
-    (src/cdmf_cuda_shim.cpp) compiles against include/cdmf_cuda.h and links
-    against the library, as printed there."""
+    """The C++ shim a maintainer of the reference adds as
+    src/cdmf_cuda_shim.cpp (tests/native/cdmf_cuda_shim.cpp) compiles against
+    include/cdmf_cuda.h and stand-ins for the reference's types
+    (tests/native/ref_standins), and links against the library."""
     import subprocess
     from cdmf_gb300 import _build
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = re.findall(r"```cpp\n(.*?)```", doc, flags=re.S)
-    shim = [b for b in blocks if "cdmf_cuda_train" in b]
-    assert len(shim) == 1, "one C++ block with the cdmf_cuda_train shim"
-    for name, text in _REFERENCE_STANDINS.items():
-        (tmp_path / name).write_text(text)
-    src = tmp_path / "cdmf_cuda_shim.cpp"
-    src.write_text(shim[0] + "\nint main() { return 0; }\n")
+    native = os.path.join(ROOT, "tests", "native")
+    src = tmp_path / "shim_main.cpp"
+    src.write_text('#include "%s"\nint main() { return 0; }\n' % os.path.join(native, "cdmf_cuda_shim.cpp"))
     out = tmp_path / "shim"
-    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", str(tmp_path), "-I",
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(native, "ref_standins"), "-I",
                         os.path.join(ROOT, "include"), str(src), "-o", str(out), "-L", os.path.dirname(_build.LIB),
                         "-lcdmf_cuda", "-Wl,-rpath," + os.path.dirname(_build.LIB)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-
-
-def test_integration_python_example_parses_and_names_real_functions():
-    """The Python example in INTEGRATION.md is valid Python and calls
-    functions the package has."""
-    import ast
-    from cdmf_gb300 import formats, synth
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = re.findall(r"```python\n(.*?)```", doc, flags=re.S)
-    assert blocks
-    mods = {"engine": engine, "formats": formats, "synth": synth}
-    for b in blocks:
-        tree = ast.parse(b)
-        for node in ast.walk(tree):
-            if isinstance(node, ast.Attribute) and isinstance(node.value, ast.Name) and node.value.id in mods:
-                assert hasattr(mods[node.value.id], node.attr), f"{node.value.id}.{node.attr}"

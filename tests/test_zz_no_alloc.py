@@ -1,9 +1,10 @@
 """The allocation-free test-RMSE entry point (cdmf_cuda_rmse_coo_noalloc).
 
 It serves callers that cannot let the library call cudaMalloc, such as a
-process that owns all of its device memory through its own pool, or work
-recorded into a stream capture.  The caller hands in device arrays it already
-owns.  The kernel's scratch sits in a fixed device array inside the library.
+process that hands out all of its device memory from its own pool, or a
+runtime whose device memory budget is fixed at start-up.  The caller hands in
+device arrays it already owns.  The kernel's scratch sits in a fixed device
+array inside the library.
 This file checks, through the C ABI, that the result matches the allocating
 entry point (cdmf_cuda_rmse_coo) on two calls in a row and on calls of
 different sizes: the shared scratch must not carry one call's values into the
