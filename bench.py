@@ -13,10 +13,15 @@ Printed as one JSON line (rank 0):
             with a per-iteration RMSE read-back, download of W and H
   roofline -- the sweep kernel: compulsory bytes per launch / mean launch time
   cpu_baseline -- the oracle CPU port of the reference engine on the host cores
+  batch64 -- the 64 uneven problems in one batched run against the same
+            problems run one after another (--no-batch leaves it out)
 
 --impl reference: the reference's CPU engine (oracle port; the reference
-sources are not on the GPU host) on the same workload, one bounded sample per
-step, all host threads.
+sources are not on the GPU host) on the same workload and config, all host
+threads: W outer iterations untimed, then K timed ones, each k rank-one
+updates and the test RMSE, as the GPU arm's steps.  It loads the oracle
+libraries only (the matrix comes from the generator built into
+oracle/libsynth.so).
 
 Multi-GPU: `torchrun --nproc-per-node N bench.py --gpus N` runs one
 independent replica per GPU (weak scaling, no collective in the data path);
@@ -154,22 +159,41 @@ def profiled_traffic():
             "dram_bytes_per_launch": int(out["traffic_bytes_per_launch"])}
 
 
-def cpu_sample(R, run, W0, threads, budget_s):
-    """Oracle port of cdmf_ref on the host cores: features of one steady-state
-    outer iteration (add-back on) until budget_s is spent.  Returns
-    (updates/s, features timed, seconds)."""
+def cpu_outer_iterations(R, run, W0, threads, n_warm, n_timed=None, budget_s=None):
+    """The oracle port of the reference's engine (src/cdmf_ref.cpp:69-137) on
+    the host cores, with OpenMP over `threads`: whole outer iterations (k
+    rank-one updates, then the test RMSE of src/tools.cpp:543-582) from W0,
+    H = 0.  n_warm iterations untimed, then n_timed timed ones (or, with
+    budget_s, timed ones until that many seconds are spent, at least one).
+    Returns (seconds per timed iteration, test RMSE after each)."""
     from oracle import oracle
-    k = run["k"]
-    done, spent = 0, 0.0
+    k, lam, T = run["k"], run["lambda_"], run["maxinneriter"]
+    W = np.ascontiguousarray(W0, np.float32).copy()
+    H = np.zeros((k, R.n), np.float32)
     rc, rr = R.csc_val.copy(), R.csr_val.copy()
-    H = np.zeros((1, R.n), np.float32)
-    while done < k and (spent < budget_s or done == 0):
-        W = np.ascontiguousarray(W0[done:done + 1])
+    oiter = 1
+    for _ in range(n_warm):
+        oracle.outer_iteration(R, W, H, rc, rr, k, lam, T, oiter, threads=threads)
+        oracle.rmse(R, W, H, k)
+        oiter += 1
+    secs, rms = [], []
+    while (n_timed is not None and len(secs) < n_timed) or (
+            n_timed is None and (not secs or sum(secs) < budget_s)):
         t0 = time.perf_counter()
-        oracle.outer_iteration(R, W, H, rc, rr, 1, run["lambda_"], run["maxinneriter"], 2, threads=threads)
-        spent += time.perf_counter() - t0
-        done += 1
-    return done / spent, done, spent
+        oracle.outer_iteration(R, W, H, rc, rr, k, lam, T, oiter, threads=threads)
+        rms.append(oracle.rmse(R, W, H, k))
+        secs.append(time.perf_counter() - t0)
+        oiter += 1
+    return secs, rms
+
+
+def workload_config(R, run, ws):
+    """The `config` of both arms: the same workload, step and L2 policy."""
+    return {"workload": f"{WORKLOAD} {R.m}x{R.n} train_nnz={R.nnz} test_nnz={R.nnz_test} k={run['k']} "
+                        f"lambda={run['lambda_']} T={run['maxinneriter']}",
+            "step": "one outer iteration (k rank-one updates + test RMSE)",
+            "l2": "no flush: the residual copies streamed every feature exceed L2",
+            "parallelism": f"replicas x{ws}"}
 
 
 def main():
@@ -191,11 +215,14 @@ def main():
     ap.add_argument("--layout", default="lines", choices=["lines", "blocked"],
                     help="residual copy layout: lines (binned sweeps) or blocked (shared-memory gather tables)")
     ap.add_argument("--e2e-outer", type=int, default=20)
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--quick", action="store_true", help="device-resident timing only (no e2e, no CPU leg)")
     ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batch64"],
                     help="batch64: 64 uneven problems in one batched run vs per-problem runs")
+    ap.add_argument("--batch-residual", default="f16", choices=["f32", "bf16", "f16"],
+                    help="residual storage of the 64-problem batch (FP16: within 1e-3 of FP64 on all 64)")
+    ap.add_argument("--no-batch", action="store_true", help="leave the 64-problem batch out of the headline run")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     args.warmup = max(3, args.warmup)
@@ -210,29 +237,26 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        from oracle import oracle  # noqa: F401
-        R, run = synth.config(WORKLOAD, threads=threads)
+        # the oracle libraries only: the generator built into oracle/libsynth.so
+        # makes the same matrix as the engine library's copy
+        from oracle import oracle
+        R, run = synth.config(WORKLOAD, threads=threads, lib=oracle.synth_lib())
         run["k"] = args.k
         W0 = synth.initial_w(run["k"], R.m, seed=0)
-        for _ in range(args.warmup):
-            cpu_sample(R, run, W0, threads, 0.0)
-        vals, feats, secs = [], 0, 0.0
-        for _ in range(args.steps):
-            v, f, s = cpu_sample(R, run, W0, threads, max(1.0, args.cpu_budget / max(1, args.steps)))
-            vals.append(v)
-            feats += f
-            secs += s
-        value = feats / secs
+        secs, rms = cpu_outer_iterations(R, run, W0, threads, n_warm=args.warmup, n_timed=args.steps)
+        value = run["k"] * len(secs) / sum(secs)
         line = {
             "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded, Netflix-shaped)",
-            "config": {"workload": f"{WORKLOAD} {R.m}x{R.n} nnz={R.nnz} k={run['k']} lambda={run['lambda_']} "
-                                   f"T={run['maxinneriter']}", "sample": "features of one outer iteration"},
+            "data": "synthetic (seeded, Netflix-shaped; the data set itself is not available)",
+            "config": workload_config(R, run, ws),
+            "test_rmse": rms[-1],
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{feats} rank-one updates of a steady-state outer iteration on the full "
-                                       f"matrix, {secs:.1f} s, OpenMP over {threads} threads"},
+                             "sample": f"outer iterations {args.warmup + 1}-{args.warmup + args.steps} "
+                                       f"({run['k']} rank-one updates and the test RMSE each) on the full "
+                                       f"matrix, {sum(secs):.1f} s, oracle port of src/cdmf_ref.cpp, "
+                                       f"OpenMP over {threads} threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line), flush=True)
@@ -298,12 +322,16 @@ def main():
     fmt = None
     if not args.quick and rank == 0:
         fmt = measure_formats(R, peak)
+    batch = None
+    if not args.quick and not args.no_batch and rank == 0:
+        batch = measure_batch(args, threads, args.batch_residual)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        v, f, s = cpu_sample(R, run, W0, threads, args.cpu_budget)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{f} rank-one updates of a steady-state outer iteration (k={k}) on the full matrix, "
-                         f"{s:.1f} s, oracle port of src/cdmf_ref.cpp, OpenMP over {threads} threads"}
+        secs, _ = cpu_outer_iterations(R, run, W0, threads, n_warm=1, budget_s=args.cpu_budget)
+        cpu = {"value": k * len(secs) / sum(secs), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"outer iterations 2-{len(secs) + 1} ({k} rank-one updates and the test RMSE each) "
+                         f"on the full matrix, {sum(secs):.1f} s, oracle port of src/cdmf_ref.cpp, OpenMP "
+                         f"over {threads} threads"}
     dist.close()
     if rank != 0:
         return
@@ -313,13 +341,9 @@ def main():
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if args.residual == "f32" else f"{args.residual} residual, f32 factors and accumulation",
         "data": "synthetic (seeded, Netflix-shaped; the data set itself is not available)",
-        "config": {"workload": f"{WORKLOAD} {R.m}x{R.n} train_nnz={R.nnz} test_nnz={R.nnz_test} k={k} "
-                               f"lambda={lam} T={T}",
-                   "residual": args.residual, "version": args.version, "cuda_graph": bool(args.graph),
-                   "relabel": bool(args.relabel), "layout": args.layout, "autotune": bool(args.autotune),
-                   "step": "one outer iteration (k rank-one updates + test RMSE)",
-                   "l2": "no flush: the residual copies streamed every feature exceed L2",
-                   "parallelism": f"replicas x{ws}"},
+        "config": workload_config(R, run, ws),
+        "engine": {"residual": args.residual, "version": args.version, "cuda_graph": bool(args.graph),
+                   "relabel": bool(args.relabel), "layout": args.layout, "autotune": bool(args.autotune)},
         "outer_per_s": 1e3 * args.steps / t_ms,
         "hbm_gbs_sweeps": achieved,
         "test_rmse": test_rmse,
@@ -345,13 +369,16 @@ def main():
     if fmt is not None:
         line["formats"] = fmt
     line["rmse_ms_per_outer"] = head["rmse_ms_per_outer"]
+    if batch is not None:
+        line["batch64"] = batch
     print(json.dumps(line), flush=True)
 
 
-def bench_batch(args, threads):
-    """64 independent problems (sizes, k and lambda drawn per problem, BF16
-    residual, 10 x 1): one batched run (grouped persistent sweeps, one CUDA
-    graph) against the same problems run one after another."""
+def measure_batch(args, threads, residual):
+    """64 independent problems (sizes, k and lambda drawn per problem, 10 x 1):
+    one batched run (grouped persistent sweeps, one CUDA graph) against the
+    same problems run one after another through their own handles.  Returns
+    the batch's measurement as a dict."""
     from cdmf_gb300 import engine, synth
     specs = synth.batch_specs(64, seed=0)
     probs = [synth.generate(threads=threads, **sp["matrix"]) for sp in specs]
@@ -359,7 +386,7 @@ def bench_batch(args, threads):
     W0s = [synth.initial_w(r["k"], R.m, seed=q) for q, (R, r) in enumerate(zip(probs, runs))]
     n_outer = 10
     t_create = time.perf_counter()
-    with engine.Batch(probs, runs, maxiter=n_outer, maxinneriter=1, residual=args.residual,
+    with engine.Batch(probs, runs, maxiter=n_outer, maxinneriter=1, residual=residual,
                       use_graph=bool(args.graph), autotune=bool(args.autotune)) as b:
         t_create = time.perf_counter() - t_create
         for _ in range(args.warmup):
@@ -381,11 +408,10 @@ def bench_batch(args, threads):
     updates = sum(r["k"] for r in runs) * n_outer
     tb = statistics.median(t_batch)
     tsq = statistics.median(t_seq) if t_seq else None
-    line = {
+    return {
         "metric": "batched CCD++ rank-one updates/s (64 uneven problems)", "value": updates / (tb / 1e3),
-        "unit": "rank-one updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": tb, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": f"{args.residual} residual, f32 factors and accumulation",
+        "unit": "rank-one updates/s", "ms_per_run": tb, "runs_timed": args.steps,
+        "residual": residual,
         "data": "synthetic (seeded): m logU[1k,200k], n logU[500,20k], nnz logU[50k,5M] <= 30% fill",
         "config": {"workload": "batch64", "problems": 64, "total_train_nnz": int(sum(R.nnz for R in probs)),
                    "outer": n_outer, "inner": 1, "step": "one batched run of 10 outer iterations",
@@ -395,6 +421,15 @@ def bench_batch(args, threads):
         "rmse_equal_to_sequential": bool(np.array_equal(rm, rs)) if rs is not None else None,
         "gpu_launches": st["launches"], "clocks": clk.summary(),
     }
+
+
+def bench_batch(args, threads):
+    """--workload batch64: the batch measurement as its own JSON line."""
+    b = measure_batch(args, threads, args.batch_residual)
+    line = {"metric": b["metric"], "value": b["value"], "unit": b["unit"], "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": b["ms_per_run"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": f"{b['residual']} residual, f32 factors and accumulation"}
+    line.update({k: v for k, v in b.items() if k not in line})
     print(json.dumps(line), flush=True)
 
 

@@ -3,7 +3,8 @@
 The reference measured on Netflix, MovieLens-20M and Jester
 (SomeResults/*-GPU0{2,3}); those data sets are not available, so seeded
 synthetic matrices with their shapes, sizes and value distributions stand in
-for them.  Generation runs in libcdmf_cuda.so (include/cdmf_synth.h).
+for them.  Generation runs in libcdmf_cuda.so (include/cdmf_synth.h), or in
+any other library built from the same generator source.
 """
 import ctypes
 import math
@@ -67,9 +68,11 @@ CONFIGS = {
 }
 
 
-def generate(threads=0, seed=0, **matrix):
-    """Generates one matrix; keyword arguments are cdmf_synth_spec fields."""
-    lib = _lib.load()
+def generate(threads=0, seed=0, lib=None, **matrix):
+    """Generates one matrix; keyword arguments are cdmf_synth_spec fields.
+    `lib`: a library exporting the cdmf_synth_* functions (default: the
+    engine library)."""
+    lib = lib or _lib.load()
     sp = spec(seed=seed, **matrix)
     h = ctypes.c_void_p()
     _lib.check(lib.cdmf_synth_create(ctypes.byref(sp), int(threads), ctypes.byref(h)), "cdmf_synth_create")
@@ -90,12 +93,12 @@ def generate(threads=0, seed=0, **matrix):
     return RatingMatrix(m, n, **a)
 
 
-def config(name, threads=0, seed=0, **overrides):
+def config(name, threads=0, seed=0, lib=None, **overrides):
     """(matrix, run-parameters) of a named workload; overrides patch the matrix spec."""
     c = CONFIGS[name]
     mspec = dict(c["matrix"])
     mspec.update(overrides)
-    return generate(threads=threads, seed=seed, **mspec), dict(c["run"])
+    return generate(threads=threads, seed=seed, lib=lib, **mspec), dict(c["run"])
 
 
 def batch_specs(count=64, seed=0):

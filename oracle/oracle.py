@@ -124,6 +124,31 @@ def objective(R, W, H, res, lam):
     return sq, reg, sq + reg
 
 
+_SYNTH = []
+
+
+def synth_lib():
+    """The seeded matrix generator (include/cdmf_synth.h) as oracle/libsynth.so,
+    for callers that must not load the engine library (the benchmark's CPU
+    reference arm); it makes the same matrices as the engine library's copy."""
+    if not _SYNTH:
+        path = os.path.join(HERE, "libsynth.so")
+        if not os.path.exists(path):
+            build()
+        lib = ctypes.CDLL(path)
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        lib.cdmf_synth_create.argtypes = [vp, i, vp]
+        lib.cdmf_synth_create.restype = i
+        lib.cdmf_synth_info.argtypes = [vp, vp, vp, vp, vp]
+        lib.cdmf_synth_info.restype = i
+        lib.cdmf_synth_copy.argtypes = [vp] * 10
+        lib.cdmf_synth_copy.restype = i
+        lib.cdmf_synth_destroy.argtypes = [vp]
+        lib.cdmf_synth_destroy.restype = None
+        _SYNTH.append(lib)
+    return _SYNTH[0]
+
+
 _MODEL = []
 STORAGE = {"f32": 0, "bf16": 1, "f16": 2}
 

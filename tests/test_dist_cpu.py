@@ -59,19 +59,26 @@ def test_reference_arm_other_ranks_do_no_work():
 
 def test_reference_arm_contract_line():
     """Rank 0 of the reference arm (the oracle port of cdmf_ref on the host
-    cores, a bounded sample of the Netflix-shaped workload) prints one JSON
-    line with the keys the benchmark contract asks for."""
+    cores, whole outer iterations of the Netflix-shaped workload; k = 4 here
+    to keep the test short) prints one JSON line with the keys the benchmark
+    contract asks for and the GPU arm's config, and never loads the engine
+    library."""
     import json
     env = dict(os.environ, RANK="0", LOCAL_RANK="0", WORLD_SIZE="1", MASTER_ADDR="127.0.0.1")
-    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "3", "--cpu-budget", "0"], capture_output=True, text=True, timeout=600, env=env)
+    script = ("import runpy, sys\n"
+              "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3', '--k', '4']\n"
+              "runpy.run_path(%r, run_name='__main__')\n"
+              "print('maps', open('/proc/self/maps').read().count('libcdmf_cuda'))\n" % os.path.join(ROOT, "bench.py"))
+    p = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
     assert p.returncode == 0, p.stderr
     lines = [ln for ln in p.stdout.splitlines() if ln.strip()]
-    assert len(lines) == 1, p.stdout
+    assert len(lines) == 2 and lines[1] == "maps 0", p.stdout
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "rank-one updates/s" and d["higher_is_better"] is True
     assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3 and d["n_gpus"] == 1
-    assert "480189x17770" in d["config"]["workload"] and "k=64" in d["config"]["workload"]
+    assert "480189x17770" in d["config"]["workload"] and "k=4" in d["config"]["workload"]
+    assert set(d["config"]) == {"workload", "step", "l2", "parallelism"}
+    assert 0.5 < d["test_rmse"] < 2.0
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
