@@ -44,25 +44,22 @@ def _run_parallel(cmds):
         raise RuntimeError("native build failed:\n" + msg)
 
 
-def build(verbose=False, defines=(), lib_path=None, obj_dir=None, with_cli=True):
-    """Compiles every translation unit and links the library and the CLI.
-    `defines` (e.g. ["CDMF_CHUNKS=4"]) and `lib_path` build a variant of the
-    CUDA library elsewhere (used for tuning sweeps)."""
-    obj_dir = obj_dir or OBJDIR
-    lib = lib_path or LIB
+def build(verbose=False, with_cli=True):
+    """Compiles every translation unit and links the library and the CLI."""
+    obj_dir = OBJDIR
+    lib = LIB
     os.makedirs(obj_dir, exist_ok=True)
     os.makedirs(os.path.dirname(lib), exist_ok=True)
     os.makedirs(BINDIR, exist_ok=True)
     cmds, objs = [], []
-    dflags = ["-D" + d for d in defines]
     for src in CU_SOURCES:
         obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
-        cmds.append([NVCC] + NVFLAGS + dflags + ["-c", os.path.join(CSRC, src), "-o", obj])
+        cmds.append([NVCC] + NVFLAGS + ["-c", os.path.join(CSRC, src), "-o", obj])
         objs.append(obj)
     for src, rt, part in CU_VARIANTS:
         obj = os.path.join(obj_dir, "launch_rt%d_part%d.o" % (rt, part))
-        cmds.append([NVCC] + NVFLAGS + dflags + ["-DCDMF_LAUNCH_RT=%d" % rt, "-DCDMF_LAUNCH_PART=%d" % part,
-                                                 "-c", os.path.join(CSRC, src), "-o", obj])
+        cmds.append([NVCC] + NVFLAGS + ["-DCDMF_LAUNCH_RT=%d" % rt, "-DCDMF_LAUNCH_PART=%d" % part,
+                                        "-c", os.path.join(CSRC, src), "-o", obj])
         objs.append(obj)
     for src in CXX_SOURCES:
         obj = os.path.join(obj_dir, os.path.basename(src) + ".o")

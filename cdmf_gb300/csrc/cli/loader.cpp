@@ -147,7 +147,9 @@ static void exit_with_help() {
            "    -q verbose: show information or not (default 0)\n"
            "    -p predict: test RMSE from the meta/test.txt files after training (default 0)\n"
            "    -r compare: re-run in reference summation order and compare (default 0)\n"
-           "    -V version: 1/2 row-length-binned sweeps, 3 nnz-balanced tiles (default 1)\n"
+           "    -V version: 1 row-length-binned sweeps; 2 the same engine (an alias kept for\n"
+           "       the reference's scripts: the bins already give short lines lane groups and\n"
+           "       long lines warps or CTAs); 3 nnz-balanced tiles (default 1)\n"
            "    -nBlocks: accepted, unused (grids are sized by the engine)\n"
            "    -nThreadsPerBlock: accepted, unused (default 32)\n"
            "    -residual f32|bf16|f16: residual storage precision (default f32)\n"

@@ -104,7 +104,9 @@ int main(int argc, char** argv) {
     initial_col(H_ref, param.k, R.cols);
     switch (param.version) {
         case 1: std::cout << "[info] Picked Version 1: Native" << std::endl; break;
-        case 2: std::cout << "[info] Picked Version 2: Thread Batching" << std::endl; break;
+        case 2:   // the binned sweeps of version 1; the line keeps the reference's prefix for its scripts
+            std::cout << "[info] Picked Version 2: Thread Batching (the binned sweeps of version 1)" << std::endl;
+            break;
         case 3: std::cout << "[info] Picked Version 3: Load Balancing" << std::endl; break;
         default: printf("[FAILED] Wrong version"); return EXIT_FAILURE;
     }

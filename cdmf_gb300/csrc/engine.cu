@@ -102,41 +102,22 @@ constexpr int64_t kLargeNnz = 16 << 20;
 // interleaved layout (the whole line in flight): the 64-problem batch
 // measured 169 -> 161 ms; the Netflix-shaped matrix -1 %, so not there.
 constexpr uint32_t kGroupShort = 32;
-#ifndef CDMF_GROUP_MAX
-#define CDMF_GROUP_MAX 256
-#endif
-#ifndef CDMF_WARP_MAX
-#define CDMF_WARP_MAX 2048
-#endif
-#ifndef CDMF_CTA_MAX
-#define CDMF_CTA_MAX 16384
-#endif
-#ifndef CDMF_SPLIT_CHUNK
-#define CDMF_SPLIT_CHUNK 8192
-#endif
-#ifndef CDMF_WARP_MAX_LARGE
-#define CDMF_WARP_MAX_LARGE 16384
-#endif
-#ifndef CDMF_SPLIT_CHUNK_LARGE
-#define CDMF_SPLIT_CHUNK_LARGE 16384
-#endif
-#ifndef CDMF_CTA_MAX_LARGE
-#define CDMF_CTA_MAX_LARGE 65536
-#endif
+// 16-bit modes: features between refreshes in the first outer iteration.
+constexpr uint32_t kEarlyRefresh = 32;
 struct BinCfg {
-    uint32_t thread_max = 12;               // <= : one thread per line
-    uint32_t group_max = CDMF_GROUP_MAX;    // <= : one 8-lane group per line
-    uint32_t warp_max = CDMF_WARP_MAX;      // <= : one warp per line
-    uint32_t cta_max = CDMF_CTA_MAX;        // <= : one CTA per line; above: split
-    uint32_t chunk = CDMF_SPLIT_CHUNK;      // nonzeros per chunk of a split line
+    uint32_t thread_max = 12;     // <= : one thread per line
+    uint32_t group_max = 256;     // <= : one lane group per line
+    uint32_t warp_max = 2048;     // <= : one warp per line
+    uint32_t cta_max = 16384;     // <= : one CTA per line; above: split
+    uint32_t chunk = 8192;        // nonzeros per chunk of a split line
 };
 
 BinCfg default_bins(int64_t nnz) {
     BinCfg c;
     if (nnz >= kLargeNnz) {
-        c.warp_max = CDMF_WARP_MAX_LARGE;
-        c.cta_max = CDMF_CTA_MAX_LARGE;
-        c.chunk = CDMF_SPLIT_CHUNK_LARGE;
+        c.warp_max = 16384;
+        c.cta_max = 65536;
+        c.chunk = 16384;
     }
     return c;
 }
@@ -872,14 +853,25 @@ int need_csc_pos(cdmf_handle* h) {
     return CDMF_OK;
 }
 
-// One outer iteration (src/cdmf_ref.cpp:69-137): refresh (16-bit modes),
+// Whether the 16-bit modes refresh the residual before feature t of outer
+// iteration oiter: at the start of every outer iteration after the first,
+// and every kEarlyRefresh features of the first, where no refresh has run
+// yet and every rank-one update rounds each residual entry once more.
+bool refresh_before(const cdmf_handle* h, int oiter, uint32_t t) {
+    if (h->rt == 0 || h->nnz == 0) return false;
+    if (oiter > 1) return t == 0;
+    return t > 0 && t % kEarlyRefresh == 0;
+}
+
+// One outer iteration (src/cdmf_ref.cpp:69-137): refreshes (16-bit modes),
 // k rank-one updates, test RMSE into rmse_dst.
 int do_outer(cdmf_handle* h, int oiter, double* rmse_dst) {
     int r;
-    if (h->rt != 0 && oiter > 1 && h->nnz > 0)
-        if ((r = refresh_residual(h))) return r;
-    for (uint32_t t = 0; t < h->o.k; ++t)
+    for (uint32_t t = 0; t < h->o.k; ++t) {
+        if (refresh_before(h, oiter, t))
+            if ((r = refresh_residual(h))) return r;
         if ((r = feature_step(h, t, oiter))) return r;
+    }
     if (h->o.rmse_each_outer && h->nt > 0)
         if ((r = launch_rmse(h, rmse_dst))) return r;
     return CDMF_OK;
@@ -889,7 +881,8 @@ int do_outer(cdmf_handle* h, int oiter, double* rmse_dst) {
 // depends only on (first outer, pending feature, P validity, refresh, RMSE),
 // so one graph per signature is captured on first use and replayed after.
 int do_outer_graph(cdmf_handle* h, int oiter, double* rmse_dst) {
-    const bool want_refresh = h->rt != 0 && oiter > 1 && h->nnz > 0;
+    const bool want_refresh =
+        refresh_before(h, oiter, 0) || (h->o.k > kEarlyRefresh && refresh_before(h, oiter, kEarlyRefresh));
     const bool want_rmse = h->o.rmse_each_outer && h->nt > 0;
     const int sig[5] = {oiter == 1, h->pending, h->p_for, want_refresh, want_rmse};
     cdmf_handle::Graph* G = nullptr;
@@ -922,7 +915,7 @@ int do_outer_graph(cdmf_handle* h, int oiter, double* rmse_dst) {
     } else {
         h->pending = G->end_pending;
         h->p_for = G->end_p_for;
-        if (want_refresh) h->refreshed = true;
+        if (G->refresh > 0) h->refreshed = true;
         h->st.launches += G->launches;
         h->st.sweep_csc_launches += G->csc;
         h->st.sweep_csr_launches += G->csr;
@@ -1788,6 +1781,7 @@ struct BatchOp {
     int slot;         // RMSE slot
     // GREFRESH / GRMSE: grid sizes; GREFRESH's transposes (second descriptor list)
     uint32_t blocks = 0, desc2_off = 0, nq2 = 0, prefix2_off = 0, blocks2 = 0;
+    std::vector<int> qs;  // GREFRESH: the problems refreshed
 };
 
 // Descriptor lists of the grouped (all-problem) launches of one batched run.
@@ -1845,8 +1839,13 @@ int bfail(cdmf_batch* b, int code, const std::string& msg) {
             return bfail(b, CDMF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// Host plan of n_outer lockstep outer iterations (state of the handles is
-// simulated and restored).
+// Host plan of n_outer lockstep outer iterations (the state of the handles
+// is simulated and restored).  Every problem follows the single-problem
+// engine's schedule, refreshes included, so the results are bit-identical to
+// single runs.  (Measured: running the problems in waves whose sweep bytes
+// fit in L2, each wave through all its outer iterations before the next, is
+// slower -- 195 / 237 / 288 ms against 159 ms for waves of 128 / 64 / 32 MB on
+// the 64-problem workload: the launches multiply and each carries a tail.)
 void plan_batch(cdmf_batch* B, int n_outer, std::vector<BatchOp>& ops, BatchPlan& plan) {
     std::vector<SweepArgs>& descs = plan.descs;
     std::vector<uint32_t>& prefix = plan.prefix;
@@ -1855,124 +1854,135 @@ void plan_batch(cdmf_batch* B, int n_outer, std::vector<BatchOp>& ops, BatchPlan
     std::vector<Saved> saved(P);
     for (int q = 0; q < P; ++q) saved[q] = {B->hs[q]->pending, B->hs[q]->p_for, B->hs[q]->next_oiter};
     uint32_t queues = 0;
-    for (int o = 0; o < n_outer; ++o) {
-        const int oiter = B->hs[0]->next_oiter;
-        {   // every problem's refresh (and its row-major factor copies) in two launches
-            BatchOp op{OP_GREFRESH, -1, 0, 0, false, false, 0, (uint32_t)plan.rdescs.size(), 0, 0, 0, 0};
-            op.desc2_off = (uint32_t)plan.tdescs.size();
-            std::vector<uint32_t> rp{0}, tp{0};
-            for (int q = 0; q < P; ++q) {
-                cdmf_handle* h = B->hs[q];
-                if (!(h->rt != 0 && oiter > 1 && h->nnz > 0)) continue;
-                const int tpend = h->pending;
-                const uint32_t kq = h->kp / 4;
-                RefreshDesc D;
-                D.ptr = h->csr_ptr;
-                D.idx = h->csr_idx;
-                D.val = h->csr_val;
-                D.to_csr = h->ref_to_csr;
-                D.to_csc = h->to_csc;
-                D.m = h->m;
-                D.nnz = h->nnz;
-                D.Wrm = h->Wrm;
-                D.Hrm = h->Hrm;
-                D.kp = h->kp;
-                D.slices = kq <= kRefG ? 1 : kq <= 2 * kRefG ? 2 : kq <= 4 * kRefG ? 4 : kq <= 8 * kRefG ? 8 : 0;
-                D.res_csr = h->res_csr;
-                D.res_csc = h->res_csc;
-                D.pa = tpend >= 0 ? h->H + (size_t)tpend * h->n : nullptr;
-                D.pb = tpend >= 0 ? h->W + (size_t)tpend * h->m : nullptr;
-                D.part = h->ref_part;
-                D.counter = h->ref_count;
-                D.drift_out = h->drift_out;
-                D.nonfinite = h->nonfinite;
-                plan.rdescs.push_back(D);
-                rp.push_back(rp.back() + (uint32_t)h->ref_grid);
-                const uint32_t ty = (h->kp + 31) / 32;
-                const TransposeDesc Tw{h->W, h->Wrm, h->o.k, h->kp, h->m, (uint32_t)((h->m + 31) / 32)};
-                const TransposeDesc Th{h->H, h->Hrm, h->o.k, h->kp, h->n, (uint32_t)((h->n + 31) / 32)};
-                plan.tdescs.push_back(Tw);
-                tp.push_back(tp.back() + Tw.tiles_x * ty);
-                plan.tdescs.push_back(Th);
-                tp.push_back(tp.back() + Th.tiles_x * ty);
-                h->pending = -1;
-            }
-            op.nq = (uint32_t)(plan.rdescs.size() - op.desc_off);
-            if (op.nq) {
-                op.nq2 = (uint32_t)(plan.tdescs.size() - op.desc2_off);
-                op.prefix_off = (uint32_t)prefix.size();
-                prefix.insert(prefix.end(), rp.begin(), rp.end());
-                op.blocks = rp.back();
-                op.prefix2_off = (uint32_t)prefix.size();
-                prefix.insert(prefix.end(), tp.begin(), tp.end());
-                op.blocks2 = tp.back();
-                ops.push_back(op);
-            }
+    // the refreshes due before feature t of outer iteration oiter among the
+    // problems `qs` (and the row-major factor copies they read), in two launches
+    auto grouped_refresh = [&](const std::vector<int>& qs, int oiter, uint32_t t) {
+        BatchOp op{OP_GREFRESH, -1, 0, 0, false, false, 0, (uint32_t)plan.rdescs.size(), 0, 0, 0, 0};
+        op.desc2_off = (uint32_t)plan.tdescs.size();
+        std::vector<uint32_t> rp{0}, tp{0};
+        for (int q : qs) {
+            cdmf_handle* h = B->hs[q];
+            if (t >= h->o.k || !refresh_before(h, oiter, t)) continue;
+            const int tpend = h->pending;
+            const uint32_t kq = h->kp / 4;
+            RefreshDesc D;
+            D.ptr = h->csr_ptr;
+            D.idx = h->csr_idx;
+            D.val = h->csr_val;
+            D.to_csr = h->ref_to_csr;
+            D.to_csc = h->to_csc;
+            D.m = h->m;
+            D.nnz = h->nnz;
+            D.Wrm = h->Wrm;
+            D.Hrm = h->Hrm;
+            D.kp = h->kp;
+            D.slices = kq <= kRefG ? 1 : kq <= 2 * kRefG ? 2 : kq <= 4 * kRefG ? 4 : kq <= 8 * kRefG ? 8 : 0;
+            D.res_csr = h->res_csr;
+            D.res_csc = h->res_csc;
+            D.pa = tpend >= 0 ? h->H + (size_t)tpend * h->n : nullptr;
+            D.pb = tpend >= 0 ? h->W + (size_t)tpend * h->m : nullptr;
+            D.part = h->ref_part;
+            D.counter = h->ref_count;
+            D.drift_out = h->drift_out;
+            D.nonfinite = h->nonfinite;
+            plan.rdescs.push_back(D);
+            rp.push_back(rp.back() + (uint32_t)h->ref_grid);
+            const uint32_t ty = (h->kp + 31) / 32;
+            const TransposeDesc Tw{h->W, h->Wrm, h->o.k, h->kp, h->m, (uint32_t)((h->m + 31) / 32)};
+            const TransposeDesc Th{h->H, h->Hrm, h->o.k, h->kp, h->n, (uint32_t)((h->n + 31) / 32)};
+            plan.tdescs.push_back(Tw);
+            tp.push_back(tp.back() + Tw.tiles_x * ty);
+            plan.tdescs.push_back(Th);
+            tp.push_back(tp.back() + Th.tiles_x * ty);
+            op.qs.push_back(q);
+            h->pending = -1;
         }
-        for (uint32_t t = 0; t < B->kmax && B->T > 0; ++t) {
-            std::vector<int> part;
-            for (int q = 0; q < P; ++q)
-                if (t < B->hs[q]->o.k) part.push_back(q);
-            if (part.empty()) break;
-            const bool sub = B->hs[part[0]]->pending >= 0, add = oiter > 1;
-            for (int q : part)
-                if (B->hs[q]->p_for != (int)t) {
-                    ops.push_back({OP_PACK, q, t, 0, false, false, 0, 0, 0, 0, 0, 0});
-                    B->hs[q]->p_for = (int)t;
-                }
-            for (int it = 1; it <= B->T; ++it) {
-                const uint32_t off = (uint32_t)descs.size();
-                std::vector<SweepArgs> Bs;
-                std::vector<uint32_t> pa, pb;
-                uint32_t ca = 0, cb = 0;
-                for (int q : part) {
-                    SweepArgs A, Bq;
-                    feature_args(B->hs[q], t, it, A, Bq);
-                    descs.push_back(A);
-                    Bs.push_back(Bq);
-                    const DevBins& DA = B->hs[q]->csc;
-                    const DevBins& DB = B->hs[q]->csr;
+        op.nq = (uint32_t)(plan.rdescs.size() - op.desc_off);
+        if (op.nq) {
+            op.nq2 = (uint32_t)(plan.tdescs.size() - op.desc2_off);
+            op.prefix_off = (uint32_t)prefix.size();
+            prefix.insert(prefix.end(), rp.begin(), rp.end());
+            op.blocks = rp.back();
+            op.prefix2_off = (uint32_t)prefix.size();
+            prefix.insert(prefix.end(), tp.begin(), tp.end());
+            op.blocks2 = tp.back();
+            ops.push_back(op);
+        }
+    };
+    const int oiter0 = B->hs.empty() ? 1 : B->hs[0]->next_oiter;
+    std::vector<int> wave(P);
+    for (int q = 0; q < P; ++q) wave[q] = q;
+    {
+        uint32_t kmax = 0;
+        for (int q : wave) kmax = std::max(kmax, B->hs[q]->o.k);
+        for (int o = 0; o < n_outer; ++o) {
+            const int oiter = oiter0 + o;
+            for (uint32_t t = 0; t < kmax; ++t) {
+                grouped_refresh(wave, oiter, t);
+                if (B->T <= 0) continue;
+                std::vector<int> part;
+                for (int q : wave)
+                    if (t < B->hs[q]->o.k) part.push_back(q);
+                const bool sub = B->hs[part[0]]->pending >= 0, add = oiter > 1;
+                for (int q : part)
+                    if (B->hs[q]->p_for != (int)t) {
+                        ops.push_back({OP_PACK, q, t, 0, false, false, 0, 0, 0, 0, 0, 0});
+                        B->hs[q]->p_for = (int)t;
+                    }
+                for (int it = 1; it <= B->T; ++it) {
+                    const uint32_t off = (uint32_t)descs.size();
+                    std::vector<SweepArgs> Bs;
+                    std::vector<uint32_t> pa, pb;
+                    uint32_t ca = 0, cb = 0;
+                    for (int q : part) {
+                        SweepArgs A, Bq;
+                        feature_args(B->hs[q], t, it, A, Bq);
+                        descs.push_back(A);
+                        Bs.push_back(Bq);
+                        const DevBins& DA = B->hs[q]->csc;
+                        const DevBins& DB = B->hs[q]->csr;
+                        pa.push_back(ca);
+                        pb.push_back(cb);
+                        ca += DA.nx + DA.nc + DA.nwb + DA.ngb + DA.ntb;
+                        cb += DB.nx + DB.nc + DB.nwb + DB.ngb + DB.ntb;
+                    }
                     pa.push_back(ca);
                     pb.push_back(cb);
-                    ca += DA.nx + DA.nc + DA.nwb + DA.ngb + DA.ntb;
-                    cb += DB.nx + DB.nc + DB.nwb + DB.ngb + DB.ntb;
+                    const uint32_t offB = (uint32_t)descs.size();
+                    descs.insert(descs.end(), Bs.begin(), Bs.end());
+                    const uint32_t poA = (uint32_t)prefix.size();
+                    prefix.insert(prefix.end(), pa.begin(), pa.end());
+                    const uint32_t poB = (uint32_t)prefix.size();
+                    prefix.insert(prefix.end(), pb.begin(), pb.end());
+                    const int mA = it == 1 ? M_CSC : M_PLAIN, mB = it == 1 ? M_CSR : M_PLAIN;
+                    ops.push_back({OP_GSWEEP, -1, t, mA, sub, add, K_CSC, off, (uint32_t)part.size(), poA, queues++, 0});
+                    ops.push_back({OP_GSWEEP, -1, t, mB, sub, add, K_CSR, offB, (uint32_t)part.size(), poB, queues++, 0});
                 }
-                pa.push_back(ca);
-                pb.push_back(cb);
-                const uint32_t offB = (uint32_t)descs.size();
-                descs.insert(descs.end(), Bs.begin(), Bs.end());
-                const uint32_t poA = (uint32_t)prefix.size();
-                prefix.insert(prefix.end(), pa.begin(), pa.end());
-                const uint32_t poB = (uint32_t)prefix.size();
-                prefix.insert(prefix.end(), pb.begin(), pb.end());
-                const int mA = it == 1 ? M_CSC : M_PLAIN, mB = it == 1 ? M_CSR : M_PLAIN;
-                ops.push_back({OP_GSWEEP, -1, t, mA, sub, add, K_CSC, off, (uint32_t)part.size(), poA, queues++, 0});
-                ops.push_back({OP_GSWEEP, -1, t, mB, sub, add, K_CSR, offB, (uint32_t)part.size(), poB, queues++, 0});
-            }
-            for (int q : part) {
-                ops.push_back({OP_FINISH, q, t, 0, false, false, 0, 0, 0, 0, 0, 0});
-                feature_finish(B->hs[q], t);
-            }
-        }
-        {   // every problem's test RMSE in one launch
-            BatchOp op{OP_GRMSE, -1, 0, 0, false, false, 0, (uint32_t)plan.mdescs.size(), 0, 0, 0, o};
-            std::vector<uint32_t> mp{0};
-            for (int q = 0; q < P; ++q) {
-                cdmf_handle* h = B->hs[q];
-                if (h->o.rmse_each_outer && h->nt > 0) {
-                    RmseDesc D{h->te_row, h->te_col, h->te_val, h->nt, h->m, h->n, h->W, h->H, h->o.k,
-                               h->rmse_part, h->rmse_count, h->rmse_out + o};
-                    plan.mdescs.push_back(D);
-                    mp.push_back(mp.back() + (uint32_t)h->rmse_grid);
+                for (int q : part) {
+                    ops.push_back({OP_FINISH, q, t, 0, false, false, 0, 0, 0, 0, 0, 0});
+                    feature_finish(B->hs[q], t);
                 }
-                h->next_oiter++;
             }
-            op.nq = (uint32_t)(plan.mdescs.size() - op.desc_off);
-            if (op.nq) {
-                op.prefix_off = (uint32_t)prefix.size();
-                prefix.insert(prefix.end(), mp.begin(), mp.end());
-                op.blocks = mp.back();
-                ops.push_back(op);
+            {   // every problem's test RMSE in one launch
+                BatchOp op{OP_GRMSE, -1, 0, 0, false, false, 0, (uint32_t)plan.mdescs.size(), 0, 0, 0, o};
+                std::vector<uint32_t> mp{0};
+                for (int q : wave) {
+                    cdmf_handle* h = B->hs[q];
+                    if (h->o.rmse_each_outer && h->nt > 0) {
+                        RmseDesc D{h->te_row, h->te_col, h->te_val, h->nt, h->m, h->n, h->W, h->H, h->o.k,
+                                   h->rmse_part, h->rmse_count, h->rmse_out + o};
+                        plan.mdescs.push_back(D);
+                        mp.push_back(mp.back() + (uint32_t)h->rmse_grid);
+                    }
+                    h->next_oiter++;
+                }
+                op.nq = (uint32_t)(plan.mdescs.size() - op.desc_off);
+                if (op.nq) {
+                    op.prefix_off = (uint32_t)prefix.size();
+                    prefix.insert(prefix.end(), mp.begin(), mp.end());
+                    op.blocks = mp.back();
+                    ops.push_back(op);
+                }
             }
         }
     }
@@ -2028,11 +2038,10 @@ int execute_batch(cdmf_batch* B, const std::vector<BatchOp>& ops, const BatchPla
                 BCU(B, cudaGetLastError());
                 B->st.launches += 2;
                 B->st.refresh_launches++;
-                for (cdmf_handle* h : B->hs)   // as refresh_residual leaves each problem
-                    if (h->rt != 0 && h->nnz > 0) {
-                        h->pending = -1;
-                        h->refreshed = true;
-                    }
+                for (int q : op.qs) {   // as refresh_residual leaves each problem
+                    B->hs[q]->pending = -1;
+                    B->hs[q]->refreshed = true;
+                }
                 break;
             }
             case OP_GRMSE:
@@ -2180,7 +2189,6 @@ int cdmf_cuda_batch_run(cdmf_batch* B, int n_outer, double* rmse_out) {
             B->hs[q]->next_oiter = B->g_end[3 * q];
             B->hs[q]->pending = B->g_end[3 * q + 1];
             B->hs[q]->p_for = B->g_end[3 * q + 2];
-            if (B->hs[q]->rt != 0 && n_outer > 0) B->hs[q]->refreshed = true;
         }
         for (const BatchOp& op : ops)
             if (op.kind == OP_GSWEEP) {
@@ -2190,6 +2198,7 @@ int cdmf_cuda_batch_run(cdmf_batch* B, int n_outer, double* rmse_out) {
             } else if (op.kind == OP_GREFRESH) {
                 B->st.launches += 2;
                 B->st.refresh_launches++;
+                for (int q : op.qs) B->hs[q]->refreshed = true;
             } else if (op.kind == OP_GRMSE) {
                 B->st.launches++;
                 B->st.rmse_launches++;

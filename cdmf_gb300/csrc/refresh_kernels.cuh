@@ -56,11 +56,6 @@ static __global__ void __launch_bounds__(kBlock) to_row_major_kernel(const float
 // slices per lane (k <= 16, 32, 64, 128 -> S = 1, 2, 4, 8); S = 0 walks any
 // k.  Products are summed in a fixed order: deterministic.
 constexpr int kRefG = 4;
-#ifndef CDMF_REFRESH_UNROLL
-#define CDMF_REFRESH_UNROLL 2   // rounds whose loads are in flight together (measured: 2 > 1, 4 = 2)
-#endif
-#define CDMF_PRAGMA_(x) _Pragma(#x)
-#define CDMF_PRAGMA(x) CDMF_PRAGMA_(x)
 
 // Block `bid` of `nblk` blocks of one refresh.
 template <int RT, int S>
@@ -115,7 +110,8 @@ __device__ __forceinline__ void refresh_body(
                 v = __ldg(val + p);
             }
             float dot = 0.0f;
-            CDMF_PRAGMA(unroll CDMF_REFRESH_UNROLL)
+            // two rounds' loads in flight together (measured: 2 > 1, 4 = 2)
+#pragma unroll 2
             for (int r = 0; r < kRefG; ++r) {
                 const int src = r * kPer + gi;
                 const uint32_t ii = __shfl_sync(FULL, i, src);

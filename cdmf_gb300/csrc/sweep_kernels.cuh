@@ -46,20 +46,12 @@ namespace cdmf {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
-// Minimum resident blocks per SM asked of the compiler (register cap):
-// 6 blocks of 256 threads (at most 40 registers) measured best on the
-// 480,189 x 17,770 workload; 0 lets the compiler pick freely.
-#ifndef CDMF_SWEEP_MIN_BLOCKS
-#define CDMF_SWEEP_MIN_BLOCKS 6
-#endif
-#if CDMF_SWEEP_MIN_BLOCKS > 0
-#define CDMF_SWEEP_BOUNDS __launch_bounds__(kBlock, CDMF_SWEEP_MIN_BLOCKS)
-#else
-#define CDMF_SWEEP_BOUNDS __launch_bounds__(kBlock)
-#endif
-#ifndef CDMF_TILE_MIN_BLOCKS
-#define CDMF_TILE_MIN_BLOCKS 6
-#endif
+// Resident blocks per SM asked of the compiler (register cap): 6 blocks of
+// 256 threads (at most 40 registers) measured best on the 480,189 x 17,770
+// workload, against 4 and 5 blocks with more chunks in flight per lane.
+constexpr int kSweepBlocks = 6;
+#define CDMF_SWEEP_BOUNDS __launch_bounds__(kBlock, kSweepBlocks)
+constexpr int kTileBlocks = 6;
 
 // sweep modes
 constexpr int M_PLAIN = 0;  // inner iterations >= 2: y only, no residual writes
@@ -149,37 +141,19 @@ struct SubTeam {
 
 // ---- streaming loads -----------------------------------------------------------
 // 128-bit and 64-bit loads of the index and residual streams, evict-first
-// (read once per sweep).  CDMF_STREAM_PF = 128 or 256 adds the L2 prefetch-size
-// hint, so an L2 miss fetches that many bytes from DRAM: the next chunk of a
-// lane's stream is on its way before the lane asks for it.
-#ifndef CDMF_STREAM_PF
-#define CDMF_STREAM_PF 256   // measured: +0.9 % FP32 updates/s, neutral at BF16
-#endif
+// (read once per sweep), with the 256-byte L2 prefetch-size hint: an L2 miss
+// fetches that many bytes from DRAM, so the next chunk of a lane's stream is
+// on its way before the lane asks for it.  (Measured: +0.9 % FP32 updates/s,
+// neutral at BF16; an L1::no_allocate hint instead of evict-first: neutral.)
 __device__ __forceinline__ uint4 ld_stream4(const void* p) {
-#if CDMF_STREAM_PF == 256
     uint4 v;
     asm("ld.global.cs.L2::256B.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
     return v;
-#elif CDMF_STREAM_PF == 128
-    uint4 v;
-    asm("ld.global.cs.L2::128B.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
-    return v;
-#else
-    return __ldcs((const uint4*)p);
-#endif
 }
 __device__ __forceinline__ uint2 ld_stream2(const void* p) {
-#if CDMF_STREAM_PF == 256
     uint2 v;
     asm("ld.global.cs.L2::256B.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
     return v;
-#elif CDMF_STREAM_PF == 128
-    uint2 v;
-    asm("ld.global.cs.L2::128B.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
-    return v;
-#else
-    return __ldcs((const uint2*)p);
-#endif
 }
 
 // ---- residual element access -------------------------------------------------
@@ -236,8 +210,10 @@ template <> struct Res<1> : Res16<1> {};
 template <> struct Res<2> : Res16<2> {};
 
 // Running sum; with KAHAN the lost low-order part is carried in `c`
-// (compensated summation, used for lines longer than the warp bin when the
-// residual is stored in 16 bits).
+// (compensated summation).  With a 16-bit residual every line longer than
+// kKahanMin nonzeros sums with it: CTA and split lines always, warp lines
+// above kKahanMin.
+constexpr uint32_t kKahanMin = 4096;
 template <bool KAHAN> struct Acc {
     float s = 0.0f, c = 0.0f;
     __device__ __forceinline__ void add(float x) {
@@ -321,14 +297,8 @@ __device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, 
 // head up to the first 4-aligned position (lanes 0..2), then 4-element vector
 // chunks (chunk c to lane c mod S, kChunks chunks in flight per lane), then a
 // scalar tail.  Each lane visits its elements in increasing order.
-#ifndef CDMF_CHUNKS
-#define CDMF_CHUNKS 2
-#endif
-#ifndef CDMF_ILP
-#define CDMF_ILP 8
-#endif
-constexpr int kChunks = CDMF_CHUNKS;   // vector layout: 4-element chunks in flight per lane
-constexpr int kIlp = CDMF_ILP;         // interleaved layout: elements in flight per lane
+constexpr int kChunks = 2;   // vector layout: 4-element chunks in flight per lane
+constexpr int kIlp = 4;      // interleaved layout: elements in flight per lane
 
 // Vector layout (default; measured faster for 16-bit residuals): lane takes 4 consecutive nonzeros per 128-bit load, after a
 // scalar head that reaches a 4-aligned position, then a scalar tail.
@@ -386,10 +356,9 @@ __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, ui
 // the S lanes of one load, and of the gather that follows it, touch S
 // consecutive nonzeros -- neighbouring cross indices, few cache lines per
 // gather.  ILP nonzeros per lane are in flight per step.
-template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN, int ILP = kIlp>
+template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided_il(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
                                            float dj, float& gs, float& hs) {
-    constexpr int kIlp = ILP;
     Acc<KAHAN> g, h;
     uint32_t q = beg + lane;
     for (; q + (uint32_t)S * (kIlp - 1) < end; q += (uint32_t)S * kIlp) {
@@ -415,31 +384,21 @@ __device__ __forceinline__ void strided_il(const SweepArgs& A, uint32_t beg, uin
 
 // Thread-bin lines: loads of this many nonzeros in flight per thread
 // (measured: 4 takes the 64-problem batch from 178 to 172 ms, neutral on the
-// Netflix-shaped matrix).  8-lane group lines: CDMF_GROUP_IL > 0 switches them
-// to the interleaved layout with that many nonzeros in flight (measured slower:
-// -8 % on the Netflix-shaped matrix at 4).
-#ifndef CDMF_THREAD_UNROLL
-#define CDMF_THREAD_UNROLL 4
-#endif
-#ifndef CDMF_GROUP_IL
-#define CDMF_GROUP_IL 0
-#endif
-// 8-lane group lines of at most SweepArgs::group_short nonzeros take the
-// interleaved layout with the whole line in flight at once; longer ones the
-// vector layout.
+// Netflix-shaped matrix).
+constexpr int kThreadUnroll = 4;
+// Lane-group lines of at most SweepArgs::group_short nonzeros take the
+// interleaved layout with the whole line in flight at once; everything else
+// the vector layout.  (Measured slower: the interleaved layout for all
+// lines, -8 % on the Netflix-shaped matrix with 8-lane groups at 4 in
+// flight; 8-nonzero chunks; staging the streams through shared memory with
+// cp.async, which takes L1 capacity from the gather tables.)
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
                                         float dj, float& gs, float& hs) {
-#ifdef CDMF_INTERLEAVED_STREAMS
-    strided_il<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
-#else
-    if (CDMF_GROUP_IL > 0 && S <= 8)
-        strided_il<RT, MODE, SUB, ADD, S, KAHAN, (CDMF_GROUP_IL > 0 ? CDMF_GROUP_IL : 1)>(A, beg, end, lane, bj, dj, gs, hs);
-    else if (S <= 8 && end - beg <= A.group_short)
-        strided_il<RT, MODE, SUB, ADD, S, KAHAN, 4>(A, beg, end, lane, bj, dj, gs, hs);
+    if (S <= 8 && end - beg <= A.group_short)
+        strided_il<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
     else
         strided_vec<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
-#endif
 }
 
 template <int WIDTH = 32>
@@ -568,7 +527,10 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
         float bj, dj;
         line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
         float g = 0.0f, h = 0.0f;
-        strided<RT, MODE, SUB, ADD, 32, false>(A, beg, end, lane, bj, dj, g, h);
+        if (RT != 0 && end - beg > kKahanMin)
+            strided<RT, MODE, SUB, ADD, 32, true>(A, beg, end, lane, bj, dj, g, h);
+        else
+            strided<RT, MODE, SUB, ADD, 32, false>(A, beg, end, lane, bj, dj, g, h);
         warp_sum2(g, h);
         if (lane == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
         return;
@@ -601,25 +563,23 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
     Acc<false> g, h;
     h.s = __fmul_rn(A.lambda, __uint2float_rn(len));         // h starts at lambda*nnz (src/cdmf_ref.cpp:8)
     uint32_t q = beg;
-#if CDMF_THREAD_UNROLL > 1
-    // loads of CDMF_THREAD_UNROLL nonzeros in flight; sums still in index order
-    for (; q + CDMF_THREAD_UNROLL <= end; q += CDMF_THREAD_UNROLL) {
-        uint32_t iv[CDMF_THREAD_UNROLL];
-        float r[CDMF_THREAD_UNROLL];
+    // loads of kThreadUnroll nonzeros in flight; sums still in index order
+    for (; q + kThreadUnroll <= end; q += kThreadUnroll) {
+        uint32_t iv[kThreadUnroll];
+        float r[kThreadUnroll];
 #pragma unroll
-        for (int e = 0; e < CDMF_THREAD_UNROLL; ++e) {
+        for (int e = 0; e < kThreadUnroll; ++e) {
             iv[e] = ld_idx1<MODE>(A, q + e);
             r[e] = Res<RT>::ld(A.res, q + e);
         }
 #pragma unroll
-        for (int e = 0; e < CDMF_THREAD_UNROLL; ++e) {
+        for (int e = 0; e < kThreadUnroll; ++e) {
             float a, c, y;
             fetch<MODE>(A, iv[e], a, c, y);
             if (SUB || ADD) r[e] = Res<RT>::st(A.res, q + e, update<SUB, ADD>(r[e], a, c, bj, dj));
             accumulate(g, h, y, r[e]);
         }
     }
-#endif
     for (; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
     write_line<MODE>(A, j, __fdiv_rn(g.s, h.s), bj, dj);
 }

@@ -29,10 +29,7 @@ namespace cdmf {
 
 // Measured on the Netflix-shaped matrix (BF16): 1,024-nonzero warp tiles and
 // 6 blocks per SM run 1,190 / 1,150 updates/s against 1,060 for 512 and 5.
-#ifndef CDMF_TILE_STEPS
-#define CDMF_TILE_STEPS 32
-#endif
-constexpr int kTileSteps = CDMF_TILE_STEPS;
+constexpr int kTileSteps = 32;
 constexpr int kWarpTile = 32 * kTileSteps;   // nonzeros per warp tile
 
 struct TileArgs {
@@ -91,7 +88,7 @@ __device__ __forceinline__ void tile_arrive(const TileArgs& T, uint32_t line, bo
 }
 
 template <int RT, int MODE, bool SUB, bool ADD>
-__global__ void __launch_bounds__(kBlock, CDMF_TILE_MIN_BLOCKS) tile_sweep_kernel(const TileArgs T) {
+__global__ void __launch_bounds__(kBlock, kTileBlocks) tile_sweep_kernel(const TileArgs T) {
     const SweepArgs& A = T.s;
     const uint32_t lane = threadIdx.x & 31;
     if (blockIdx.x >= T.tile_blocks) {                      // empty lines
