@@ -1757,70 +1757,33 @@ int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* 
 // ============================================================================
 // Batches of independent factorisations (uneven sizes, own k and lambda).
 //
-// All problems advance in lockstep.  At feature index t, every problem with
-// k > t runs its sweep, and the sweeps of all those problems run in ONE
-// persistent launch (grouped_sweep_kernel): resident blocks pull
-// (problem, bin-block) work from a device queue.  The residual refresh,
-// the packed-table setup and the test RMSE stay per problem.  The whole
-// schedule of a run is planned on the host, its sweep descriptors are
-// uploaded once, and in graph mode the run is replayed as one CUDA graph.
+// Every problem keeps its own engine handle and its own CUDA stream, and runs
+// exactly its single-problem schedule (refreshes, sweeps, test RMSE) on that
+// stream.  A batched run forks all the streams from the batch stream, issues
+// the problems' outer iterations interleaved (outer iteration by outer
+// iteration, problem by problem), and joins them back; with use_graph the
+// whole run is captured once as one CUDA graph of independent branches and
+// replayed after.  The GPU's scheduler then overlaps the problems' kernels:
+// while one problem's launch drains, the next launches of the other problems
+// fill the SMs, and each problem's data stays in L2 between its own launches.
+// Results are bit-identical to running each problem alone.  (Measured on the
+// 64-problem workload, FP16, 10 x 1: 108 ms against 159 ms for all problems
+// in lockstep, one grouped launch per half step, and 223 ms for one persistent
+// launch per outer iteration with per-problem dependencies; 370 ms one after
+// another.)
 // ============================================================================
-
-namespace {
-
-enum { OP_PACK, OP_REFRESH, OP_GSWEEP, OP_FINISH, OP_RMSE, OP_GREFRESH, OP_GRMSE };
-
-struct BatchOp {
-    int kind;
-    int q;            // problem (PACK, REFRESH, FINISH, RMSE)
-    uint32_t t;       // feature (PACK, FINISH)
-    int mode;         // GSWEEP
-    bool sub, add;
-    int side;         // K_CSC / K_CSR
-    uint32_t desc_off, nq, prefix_off, queue;
-    int slot;         // RMSE slot
-    // GREFRESH / GRMSE: grid sizes; GREFRESH's transposes (second descriptor list)
-    uint32_t blocks = 0, desc2_off = 0, nq2 = 0, prefix2_off = 0, blocks2 = 0;
-    std::vector<int> qs;  // GREFRESH: the problems refreshed
-};
-
-// Descriptor lists of the grouped (all-problem) launches of one batched run.
-struct BatchPlan {
-    std::vector<SweepArgs> descs;
-    std::vector<uint32_t> prefix;
-    std::vector<RefreshDesc> rdescs;
-    std::vector<TransposeDesc> tdescs;
-    std::vector<RmseDesc> mdescs;
-};
-
-}  // namespace
 
 struct cdmf_batch {
     std::vector<cdmf_handle*> hs;
-    cudaStream_t s = nullptr;
-    int device = 0, rt = 0, T = 1, grid = 0, use_graph = 0;
-    bool all_idx16 = false;          // every problem has 16-bit CSR indices
-    uint32_t kmax = 0;
-    SweepArgs* d_desc = nullptr;
-    SweepArgs* h_desc = nullptr;     // pinned staging
-    size_t desc_cap = 0;
-    uint32_t* d_prefix = nullptr;
-    uint32_t* h_prefix = nullptr;
-    size_t prefix_cap = 0;
-    uint32_t* d_queue = nullptr;
-    size_t queue_cap = 0;
-    RefreshDesc *d_rdesc = nullptr, *h_rdesc = nullptr;
-    size_t rdesc_cap = 0;
-    TransposeDesc *d_tdesc = nullptr, *h_tdesc = nullptr;
-    size_t tdesc_cap = 0;
-    RmseDesc *d_mdesc = nullptr, *h_mdesc = nullptr;
-    size_t mdesc_cap = 0;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaStream_t s = nullptr;        // the batch stream: fork, join, timing
+    int device = 0, use_graph = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, fork = nullptr;
+    std::vector<cudaEvent_t> joins;  // one per problem stream
     cudaGraphExec_t gexec = nullptr;
     int g_outer = -1;
     std::vector<int> g_start;        // per problem: next_oiter, pending, p_for at capture
     std::vector<int> g_end;
-    cdmf_stats g_single{};           // per-problem launches recorded while capturing
+    cdmf_stats g_single{};           // the problems' launches recorded while capturing
     cdmf_stats st{};
     std::string err;
 };
@@ -1839,238 +1802,32 @@ int bfail(cdmf_batch* b, int code, const std::string& msg) {
             return bfail(b, CDMF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// Host plan of n_outer lockstep outer iterations (the state of the handles
-// is simulated and restored).  Every problem follows the single-problem
-// engine's schedule, refreshes included, so the results are bit-identical to
-// single runs.  (Measured: running the problems in waves whose sweep bytes
-// fit in L2, each wave through all its outer iterations before the next, is
-// slower -- 195 / 237 / 288 ms against 159 ms for waves of 128 / 64 / 32 MB on
-// the 64-problem workload: the launches multiply and each carries a tail.)
-void plan_batch(cdmf_batch* B, int n_outer, std::vector<BatchOp>& ops, BatchPlan& plan) {
-    std::vector<SweepArgs>& descs = plan.descs;
-    std::vector<uint32_t>& prefix = plan.prefix;
+// Issues n_outer outer iterations of every problem, each on its own stream
+// after the fork event of the batch stream, then joins the streams back into
+// the batch stream.
+int issue_streams(cdmf_batch* B, int n_outer) {
     const int P = (int)B->hs.size();
-    struct Saved { int pending, p_for, next; };
-    std::vector<Saved> saved(P);
-    for (int q = 0; q < P; ++q) saved[q] = {B->hs[q]->pending, B->hs[q]->p_for, B->hs[q]->next_oiter};
-    uint32_t queues = 0;
-    // the refreshes due before feature t of outer iteration oiter among the
-    // problems `qs` (and the row-major factor copies they read), in two launches
-    auto grouped_refresh = [&](const std::vector<int>& qs, int oiter, uint32_t t) {
-        BatchOp op{OP_GREFRESH, -1, 0, 0, false, false, 0, (uint32_t)plan.rdescs.size(), 0, 0, 0, 0};
-        op.desc2_off = (uint32_t)plan.tdescs.size();
-        std::vector<uint32_t> rp{0}, tp{0};
-        for (int q : qs) {
+    BCU(B, cudaEventRecord(B->fork, B->s));
+    for (cdmf_handle* h : B->hs) BCU(B, cudaStreamWaitEvent(h->s, B->fork, 0));
+    for (int o = 0; o < n_outer; ++o)
+        for (int q = 0; q < P; ++q) {
             cdmf_handle* h = B->hs[q];
-            if (t >= h->o.k || !refresh_before(h, oiter, t)) continue;
-            const int tpend = h->pending;
-            const uint32_t kq = h->kp / 4;
-            RefreshDesc D;
-            D.ptr = h->csr_ptr;
-            D.idx = h->csr_idx;
-            D.val = h->csr_val;
-            D.to_csr = h->ref_to_csr;
-            D.to_csc = h->to_csc;
-            D.m = h->m;
-            D.nnz = h->nnz;
-            D.Wrm = h->Wrm;
-            D.Hrm = h->Hrm;
-            D.kp = h->kp;
-            D.slices = kq <= kRefG ? 1 : kq <= 2 * kRefG ? 2 : kq <= 4 * kRefG ? 4 : kq <= 8 * kRefG ? 8 : 0;
-            D.res_csr = h->res_csr;
-            D.res_csc = h->res_csc;
-            D.pa = tpend >= 0 ? h->H + (size_t)tpend * h->n : nullptr;
-            D.pb = tpend >= 0 ? h->W + (size_t)tpend * h->m : nullptr;
-            D.part = h->ref_part;
-            D.counter = h->ref_count;
-            D.drift_out = h->drift_out;
-            D.nonfinite = h->nonfinite;
-            plan.rdescs.push_back(D);
-            rp.push_back(rp.back() + (uint32_t)h->ref_grid);
-            const uint32_t ty = (h->kp + 31) / 32;
-            const TransposeDesc Tw{h->W, h->Wrm, h->o.k, h->kp, h->m, (uint32_t)((h->m + 31) / 32)};
-            const TransposeDesc Th{h->H, h->Hrm, h->o.k, h->kp, h->n, (uint32_t)((h->n + 31) / 32)};
-            plan.tdescs.push_back(Tw);
-            tp.push_back(tp.back() + Tw.tiles_x * ty);
-            plan.tdescs.push_back(Th);
-            tp.push_back(tp.back() + Th.tiles_x * ty);
-            op.qs.push_back(q);
-            h->pending = -1;
+            const int r = do_outer(h, h->next_oiter + o, h->rmse_out + o);
+            if (r) return bfail(B, r, h->err);
         }
-        op.nq = (uint32_t)(plan.rdescs.size() - op.desc_off);
-        if (op.nq) {
-            op.nq2 = (uint32_t)(plan.tdescs.size() - op.desc2_off);
-            op.prefix_off = (uint32_t)prefix.size();
-            prefix.insert(prefix.end(), rp.begin(), rp.end());
-            op.blocks = rp.back();
-            op.prefix2_off = (uint32_t)prefix.size();
-            prefix.insert(prefix.end(), tp.begin(), tp.end());
-            op.blocks2 = tp.back();
-            ops.push_back(op);
-        }
-    };
-    const int oiter0 = B->hs.empty() ? 1 : B->hs[0]->next_oiter;
-    std::vector<int> wave(P);
-    for (int q = 0; q < P; ++q) wave[q] = q;
-    {
-        uint32_t kmax = 0;
-        for (int q : wave) kmax = std::max(kmax, B->hs[q]->o.k);
-        for (int o = 0; o < n_outer; ++o) {
-            const int oiter = oiter0 + o;
-            for (uint32_t t = 0; t < kmax; ++t) {
-                grouped_refresh(wave, oiter, t);
-                if (B->T <= 0) continue;
-                std::vector<int> part;
-                for (int q : wave)
-                    if (t < B->hs[q]->o.k) part.push_back(q);
-                const bool sub = B->hs[part[0]]->pending >= 0, add = oiter > 1;
-                for (int q : part)
-                    if (B->hs[q]->p_for != (int)t) {
-                        ops.push_back({OP_PACK, q, t, 0, false, false, 0, 0, 0, 0, 0, 0});
-                        B->hs[q]->p_for = (int)t;
-                    }
-                for (int it = 1; it <= B->T; ++it) {
-                    const uint32_t off = (uint32_t)descs.size();
-                    std::vector<SweepArgs> Bs;
-                    std::vector<uint32_t> pa, pb;
-                    uint32_t ca = 0, cb = 0;
-                    for (int q : part) {
-                        SweepArgs A, Bq;
-                        feature_args(B->hs[q], t, it, A, Bq);
-                        descs.push_back(A);
-                        Bs.push_back(Bq);
-                        const DevBins& DA = B->hs[q]->csc;
-                        const DevBins& DB = B->hs[q]->csr;
-                        pa.push_back(ca);
-                        pb.push_back(cb);
-                        ca += DA.nx + DA.nc + DA.nwb + DA.ngb + DA.ntb;
-                        cb += DB.nx + DB.nc + DB.nwb + DB.ngb + DB.ntb;
-                    }
-                    pa.push_back(ca);
-                    pb.push_back(cb);
-                    const uint32_t offB = (uint32_t)descs.size();
-                    descs.insert(descs.end(), Bs.begin(), Bs.end());
-                    const uint32_t poA = (uint32_t)prefix.size();
-                    prefix.insert(prefix.end(), pa.begin(), pa.end());
-                    const uint32_t poB = (uint32_t)prefix.size();
-                    prefix.insert(prefix.end(), pb.begin(), pb.end());
-                    const int mA = it == 1 ? M_CSC : M_PLAIN, mB = it == 1 ? M_CSR : M_PLAIN;
-                    ops.push_back({OP_GSWEEP, -1, t, mA, sub, add, K_CSC, off, (uint32_t)part.size(), poA, queues++, 0});
-                    ops.push_back({OP_GSWEEP, -1, t, mB, sub, add, K_CSR, offB, (uint32_t)part.size(), poB, queues++, 0});
-                }
-                for (int q : part) {
-                    ops.push_back({OP_FINISH, q, t, 0, false, false, 0, 0, 0, 0, 0, 0});
-                    feature_finish(B->hs[q], t);
-                }
-            }
-            {   // every problem's test RMSE in one launch
-                BatchOp op{OP_GRMSE, -1, 0, 0, false, false, 0, (uint32_t)plan.mdescs.size(), 0, 0, 0, o};
-                std::vector<uint32_t> mp{0};
-                for (int q : wave) {
-                    cdmf_handle* h = B->hs[q];
-                    if (h->o.rmse_each_outer && h->nt > 0) {
-                        RmseDesc D{h->te_row, h->te_col, h->te_val, h->nt, h->m, h->n, h->W, h->H, h->o.k,
-                                   h->rmse_part, h->rmse_count, h->rmse_out + o};
-                        plan.mdescs.push_back(D);
-                        mp.push_back(mp.back() + (uint32_t)h->rmse_grid);
-                    }
-                    h->next_oiter++;
-                }
-                op.nq = (uint32_t)(plan.mdescs.size() - op.desc_off);
-                if (op.nq) {
-                    op.prefix_off = (uint32_t)prefix.size();
-                    prefix.insert(prefix.end(), mp.begin(), mp.end());
-                    op.blocks = mp.back();
-                    ops.push_back(op);
-                }
-            }
-        }
-    }
     for (int q = 0; q < P; ++q) {
-        B->hs[q]->pending = saved[q].pending;
-        B->hs[q]->p_for = saved[q].p_for;
-        B->hs[q]->next_oiter = saved[q].next;
+        BCU(B, cudaEventRecord(B->joins[q], B->hs[q]->s));
+        BCU(B, cudaStreamWaitEvent(B->s, B->joins[q], 0));
     }
-}
-
-template <class T>
-int grow_pair(cdmf_batch* B, T** d, T** hpin, size_t& cap, size_t need) {
-    if (need <= cap) return CDMF_OK;
-    if (*d) cudaFree(*d);
-    if (*hpin) cudaFreeHost(*hpin);
-    *d = nullptr;
-    *hpin = nullptr;
-    cap = 0;
-    if (cudaMalloc((void**)d, sizeof(T) * need) != cudaSuccess) return bfail(B, CDMF_ERR_ALLOC, "batch descriptors");
-    if (cudaHostAlloc((void**)hpin, sizeof(T) * need, cudaHostAllocDefault) != cudaSuccess)
-        return bfail(B, CDMF_ERR_ALLOC, "batch descriptors (host)");
-    cap = need;
     return CDMF_OK;
 }
 
-int execute_batch(cdmf_batch* B, const std::vector<BatchOp>& ops, const BatchPlan& plan, uint32_t nqueue) {
-    BCU(B, cudaMemcpyAsync(B->d_desc, B->h_desc, sizeof(SweepArgs) * plan.descs.size(), cudaMemcpyHostToDevice, B->s));
-    BCU(B, cudaMemcpyAsync(B->d_prefix, B->h_prefix, 4 * plan.prefix.size(), cudaMemcpyHostToDevice, B->s));
-    if (!plan.rdescs.empty()) {
-        BCU(B, cudaMemcpyAsync(B->d_rdesc, B->h_rdesc, sizeof(RefreshDesc) * plan.rdescs.size(), cudaMemcpyHostToDevice,
-                               B->s));
-        BCU(B, cudaMemcpyAsync(B->d_tdesc, B->h_tdesc, sizeof(TransposeDesc) * plan.tdescs.size(),
-                               cudaMemcpyHostToDevice, B->s));
-    }
-    if (!plan.mdescs.empty())
-        BCU(B, cudaMemcpyAsync(B->d_mdesc, B->h_mdesc, sizeof(RmseDesc) * plan.mdescs.size(), cudaMemcpyHostToDevice,
-                               B->s));
-    BCU(B, cudaMemsetAsync(B->d_queue, 0, 4 * std::max<uint32_t>(1, nqueue), B->s));
-    for (const BatchOp& op : ops) {
-        int r = CDMF_OK;
-        switch (op.kind) {
-            case OP_PACK: r = feature_prepare(B->hs[op.q], op.t); break;
-            case OP_REFRESH: r = refresh_residual(B->hs[op.q]); break;
-            case OP_FINISH: feature_finish(B->hs[op.q], op.t); break;
-            case OP_RMSE: r = launch_rmse(B->hs[op.q], B->hs[op.q]->rmse_out + op.slot); break;
-            case OP_GREFRESH: {
-                grouped_row_major_kernel<<<op.blocks2, kBlock, 0, B->s>>>(B->d_tdesc + op.desc2_off,
-                                                                          B->d_prefix + op.prefix2_off, op.nq2);
-                const RefreshDesc* d = B->d_rdesc + op.desc_off;
-                const uint32_t* pre = B->d_prefix + op.prefix_off;
-                if (B->rt == 1) grouped_refresh_kernel<1><<<op.blocks, kBlock, 0, B->s>>>(d, pre, op.nq);
-                else grouped_refresh_kernel<2><<<op.blocks, kBlock, 0, B->s>>>(d, pre, op.nq);
-                BCU(B, cudaGetLastError());
-                B->st.launches += 2;
-                B->st.refresh_launches++;
-                for (int q : op.qs) {   // as refresh_residual leaves each problem
-                    B->hs[q]->pending = -1;
-                    B->hs[q]->refreshed = true;
-                }
-                break;
-            }
-            case OP_GRMSE:
-                grouped_rmse_kernel<<<op.blocks, kBlock, 0, B->s>>>(B->d_mdesc + op.desc_off, B->d_prefix + op.prefix_off,
-                                                                    op.nq);
-                BCU(B, cudaGetLastError());
-                B->st.launches++;
-                B->st.rmse_launches++;
-                break;
-            case OP_GSWEEP: {
-                const SweepArgs* d = B->d_desc + op.desc_off;
-                const uint32_t* pre = B->d_prefix + op.prefix_off;
-                uint32_t* qu = B->d_queue + op.queue;
-                const int mode = op.mode == M_CSR && B->all_idx16 ? M_CSR16 : op.mode;
-                switch (B->rt) {
-                    case 0: grouped_rt<0>(mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
-                    case 1: grouped_rt<1>(mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
-                    default: grouped_rt<2>(mode, op.sub, op.add, d, pre, op.nq, qu, B->grid, B->s); break;
-                }
-                BCU(B, cudaGetLastError());
-                B->st.launches++;
-                if (op.side == K_CSC) B->st.sweep_csc_launches++;
-                else B->st.sweep_csr_launches++;
-                break;
-            }
-        }
-        if (r) return bfail(B, r, B->hs[op.q >= 0 ? op.q : 0]->err);
-    }
-    return CDMF_OK;
+void add_launches(cdmf_stats& to, const cdmf_stats& from) {
+    to.launches += from.launches;
+    to.sweep_csc_launches += from.sweep_csc_launches;
+    to.sweep_csr_launches += from.sweep_csr_launches;
+    to.rmse_launches += from.rmse_launches;
+    to.refresh_launches += from.refresh_launches;
 }
 
 }  // namespace
@@ -2081,23 +1838,13 @@ void cdmf_cuda_batch_destroy(cdmf_batch* B) {
     if (!B) return;
     cudaSetDevice(B->device);
     if (B->s) cudaStreamSynchronize(B->s);
-    for (cdmf_handle* h : B->hs) {
-        if (!h) continue;
-        h->s = nullptr;   // the batch stream is destroyed once, below
-        cdmf_cuda_destroy(h);
-    }
+    for (cdmf_handle* h : B->hs)
+        if (h) cdmf_cuda_destroy(h);
     if (B->gexec) cudaGraphExecDestroy(B->gexec);
-    if (B->d_desc) cudaFree(B->d_desc);
-    if (B->h_desc) cudaFreeHost(B->h_desc);
-    if (B->d_prefix) cudaFree(B->d_prefix);
-    if (B->h_prefix) cudaFreeHost(B->h_prefix);
-    if (B->d_queue) cudaFree(B->d_queue);
-    for (void* p : {(void*)B->d_rdesc, (void*)B->d_tdesc, (void*)B->d_mdesc})
-        if (p) cudaFree(p);
-    for (void* p : {(void*)B->h_rdesc, (void*)B->h_tdesc, (void*)B->h_mdesc})
-        if (p) cudaFreeHost(p);
-    if (B->e0) cudaEventDestroy(B->e0);
-    if (B->e1) cudaEventDestroy(B->e1);
+    for (cudaEvent_t e : {B->e0, B->e1, B->fork})
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : B->joins)
+        if (e) cudaEventDestroy(e);
     if (B->s) cudaStreamDestroy(B->s);
     delete B;
 }
@@ -2114,34 +1861,24 @@ int cdmf_cuda_batch_create(const cdmf_problem* probs, const cdmf_opts* opts, int
             return CDMF_ERR_UNSUPPORTED;
     cdmf_batch* B = new cdmf_batch();
     B->device = opts[0].device;
-    B->rt = opts[0].residual;
-    B->T = opts[0].maxinneriter;
     B->use_graph = opts[0].use_graph;
     auto bail = [&](int code) { cdmf_cuda_batch_destroy(B); return code; };
     if (cudaSetDevice(B->device) != cudaSuccess) return bail(CDMF_ERR_NO_DEVICE);
     if (cudaStreamCreateWithFlags(&B->s, cudaStreamNonBlocking) != cudaSuccess) return bail(CDMF_ERR_CUDA);
-    if (cudaEventCreate(&B->e0) != cudaSuccess || cudaEventCreate(&B->e1) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    if (cudaEventCreate(&B->e0) != cudaSuccess || cudaEventCreate(&B->e1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming) != cudaSuccess)
+        return bail(CDMF_ERR_CUDA);
+    B->joins.assign(nprob, nullptr);
+    for (int q = 0; q < nprob; ++q)
+        if (cudaEventCreateWithFlags(&B->joins[q], cudaEventDisableTiming) != cudaSuccess) return bail(CDMF_ERR_CUDA);
     for (int q = 0; q < nprob; ++q) {
         cdmf_opts o = opts[q];
-        o.version = 1;        // grouped sweeps use the binned kernel
-        o.use_graph = 0;
-        o.layout = CDMF_LAYOUT_LINES;
+        o.use_graph = 0;   // the batch captures the problems' launches itself
         cdmf_handle* h = nullptr;
         const int r = cdmf_cuda_create(probs + q, &o, &h);
         if (r) return bail(r);
-        cudaStreamSynchronize(h->s);
-        cudaStreamDestroy(h->s);
-        h->s = B->s;
         B->hs.push_back(h);
-        B->kmax = std::max(B->kmax, o.k);
     }
-    B->all_idx16 = !B->hs.empty();
-    for (cdmf_handle* h : B->hs)
-        if (!h->idx16) B->all_idx16 = false;
-    int per_sm = 0, sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device);
-    per_sm = grouped_blocks_per_sm();
-    B->grid = std::max(1, sms) * std::max(1, per_sm);
     *out = B;
     return CDMF_OK;
 }
@@ -2162,117 +1899,70 @@ int cdmf_cuda_batch_run(cdmf_batch* B, int n_outer, double* rmse_out) {
         if (n_outer > h->o.maxiter + 1) return bfail(B, CDMF_ERR_INVALID, "n_outer beyond the RMSE slots");
     BCU(B, cudaSetDevice(B->device));
     B->st = cdmf_stats{};
-    for (cdmf_handle* h : B->hs) {
-        h->st = cdmf_stats{};
-        h->refreshed = false;
-    }
-    std::vector<BatchOp> ops;
-    BatchPlan plan;
-    plan_batch(B, n_outer, ops, plan);
-    const std::vector<SweepArgs>& descs = plan.descs;
-    const std::vector<uint32_t>& prefix = plan.prefix;
-    uint32_t nqueue = 0;
-    for (const BatchOp& op : ops)
-        if (op.kind == OP_GSWEEP) nqueue = std::max(nqueue, op.queue + 1);
     std::vector<int> start(3 * P);
     for (int q = 0; q < P; ++q) {
-        start[3 * q] = B->hs[q]->next_oiter;
-        start[3 * q + 1] = B->hs[q]->pending;
-        start[3 * q + 2] = B->hs[q]->p_for;
+        cdmf_handle* h = B->hs[q];
+        h->st = cdmf_stats{};
+        h->refreshed = false;
+        if (h->rt != 0) BCU(B, cudaMemsetAsync(h->nonfinite, 0, 8, h->s));
+        start[3 * q] = h->next_oiter;
+        start[3 * q + 1] = h->pending;
+        start[3 * q + 2] = h->p_for;
     }
     int r;
     BCU(B, cudaEventRecord(B->e0, B->s));
-    const bool reuse = B->use_graph && B->gexec && B->g_outer == n_outer && B->g_start == start;
-    if (reuse) {
+    if (B->use_graph && B->gexec && B->g_outer == n_outer && B->g_start == start) {
         BCU(B, cudaGraphLaunch(B->gexec, B->s));
         for (int q = 0; q < P; ++q) {
-            B->hs[q]->next_oiter = B->g_end[3 * q];
             B->hs[q]->pending = B->g_end[3 * q + 1];
             B->hs[q]->p_for = B->g_end[3 * q + 2];
         }
-        for (const BatchOp& op : ops)
-            if (op.kind == OP_GSWEEP) {
-                B->st.launches++;
-                if (op.side == K_CSC) B->st.sweep_csc_launches++;
-                else B->st.sweep_csr_launches++;
-            } else if (op.kind == OP_GREFRESH) {
-                B->st.launches += 2;
-                B->st.refresh_launches++;
-                for (int q : op.qs) B->hs[q]->refreshed = true;
-            } else if (op.kind == OP_GRMSE) {
-                B->st.launches++;
-                B->st.rmse_launches++;
-            }
-        B->st.launches += B->g_single.launches;
-        B->st.rmse_launches += B->g_single.rmse_launches;
-        B->st.refresh_launches += B->g_single.refresh_launches;
+        add_launches(B->st, B->g_single);
+    } else if (B->use_graph) {
+        if (B->gexec) {
+            cudaGraphExecDestroy(B->gexec);
+            B->gexec = nullptr;
+        }
+        BCU(B, cudaStreamBeginCapture(B->s, cudaStreamCaptureModeThreadLocal));
+        r = issue_streams(B, n_outer);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(B->s, &g);
+        if (r || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return r ? r : bfail(B, CDMF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&B->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) return bfail(B, CDMF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+        B->g_outer = n_outer;
+        B->g_start = start;
+        B->g_single = cdmf_stats{};
+        for (cdmf_handle* h : B->hs) add_launches(B->g_single, h->st);
+        B->g_end.assign(3 * P, 0);
+        for (int q = 0; q < P; ++q) {
+            B->g_end[3 * q] = B->hs[q]->next_oiter + n_outer;
+            B->g_end[3 * q + 1] = B->hs[q]->pending;
+            B->g_end[3 * q + 2] = B->hs[q]->p_for;
+        }
+        add_launches(B->st, B->g_single);
+        BCU(B, cudaGraphLaunch(B->gexec, B->s));
     } else {
-        if ((r = grow_pair(B, &B->d_desc, &B->h_desc, B->desc_cap, std::max<size_t>(1, descs.size())))) return r;
-        if ((r = grow_pair(B, &B->d_prefix, &B->h_prefix, B->prefix_cap, std::max<size_t>(1, prefix.size()))))
-            return r;
-        if (nqueue > B->queue_cap) {
-            if (B->d_queue) cudaFree(B->d_queue);
-            B->d_queue = nullptr;
-            B->queue_cap = 0;
-            if (cudaMalloc((void**)&B->d_queue, 4 * (size_t)nqueue) != cudaSuccess)
-                return bfail(B, CDMF_ERR_ALLOC, "batch queues");
-            B->queue_cap = nqueue;
-        }
-        if (!B->d_queue && cudaMalloc((void**)&B->d_queue, 4) != cudaSuccess)
-            return bfail(B, CDMF_ERR_ALLOC, "batch queues");
-        if ((r = grow_pair(B, &B->d_rdesc, &B->h_rdesc, B->rdesc_cap, std::max<size_t>(1, plan.rdescs.size()))) ||
-            (r = grow_pair(B, &B->d_tdesc, &B->h_tdesc, B->tdesc_cap, std::max<size_t>(1, plan.tdescs.size()))) ||
-            (r = grow_pair(B, &B->d_mdesc, &B->h_mdesc, B->mdesc_cap, std::max<size_t>(1, plan.mdescs.size()))))
-            return r;
-        std::copy(descs.begin(), descs.end(), B->h_desc);
-        std::copy(prefix.begin(), prefix.end(), B->h_prefix);
-        std::copy(plan.rdescs.begin(), plan.rdescs.end(), B->h_rdesc);
-        std::copy(plan.tdescs.begin(), plan.tdescs.end(), B->h_tdesc);
-        std::copy(plan.mdescs.begin(), plan.mdescs.end(), B->h_mdesc);
-        if (B->use_graph) {
-            if (B->gexec) { cudaGraphExecDestroy(B->gexec); B->gexec = nullptr; }
-            BCU(B, cudaStreamBeginCapture(B->s, cudaStreamCaptureModeThreadLocal));
-            r = execute_batch(B, ops, plan, nqueue);
-            cudaGraph_t g = nullptr;
-            const cudaError_t e = cudaStreamEndCapture(B->s, &g);
-            if (r || e != cudaSuccess) {
-                if (g) cudaGraphDestroy(g);
-                return r ? r : bfail(B, CDMF_ERR_CUDA, cudaGetErrorString(e));
-            }
-            const cudaError_t ei = cudaGraphInstantiate(&B->gexec, g, 0);
-            cudaGraphDestroy(g);
-            if (ei != cudaSuccess) return bfail(B, CDMF_ERR_CUDA, cudaGetErrorString(ei));
-            B->g_outer = n_outer;
-            B->g_start = start;
-            B->g_single = cdmf_stats{};
-            for (cdmf_handle* h : B->hs) {
-                B->g_single.launches += h->st.launches;
-                B->g_single.rmse_launches += h->st.rmse_launches;
-                B->g_single.refresh_launches += h->st.refresh_launches;
-            }
-            B->g_end.assign(3 * P, 0);
-            for (int q = 0; q < P; ++q) {
-                B->hs[q]->next_oiter += n_outer;
-                B->g_end[3 * q] = B->hs[q]->next_oiter;
-                B->g_end[3 * q + 1] = B->hs[q]->pending;
-                B->g_end[3 * q + 2] = B->hs[q]->p_for;
-            }
-            BCU(B, cudaGraphLaunch(B->gexec, B->s));
-        } else {
-            if ((r = execute_batch(B, ops, plan, nqueue))) return r;
-            for (int q = 0; q < P; ++q) B->hs[q]->next_oiter += n_outer;
-        }
+        if ((r = issue_streams(B, n_outer))) return r;
+        for (cdmf_handle* h : B->hs) add_launches(B->st, h->st);
     }
+    for (cdmf_handle* h : B->hs) h->next_oiter += n_outer;
     BCU(B, cudaEventRecord(B->e1, B->s));
     BCU(B, cudaEventSynchronize(B->e1));
     float ms = 0;
     BCU(B, cudaEventElapsedTime(&ms, B->e0, B->e1));
     B->st.train_ms = ms;
-    for (cdmf_handle* h : B->hs) {
-        B->st.launches += h->st.launches;
-        B->st.rmse_launches += h->st.rmse_launches;
-        B->st.refresh_launches += h->st.refresh_launches;
-        B->st.updates += (int64_t)h->o.k * n_outer;
+    for (cdmf_handle* h : B->hs) B->st.updates += (int64_t)h->o.k * n_outer;
+    for (int q = 0; q < P; ++q) {
+        cdmf_handle* h = B->hs[q];
+        if (h->rt == 0) continue;
+        unsigned long long bad = 0;
+        BCU(B, cudaMemcpy(&bad, h->nonfinite, 8, cudaMemcpyDeviceToHost));
+        B->st.nonfinite += (int64_t)bad;
     }
     if (rmse_out)
         for (int q = 0; q < P; ++q) {
@@ -2284,6 +1974,7 @@ int cdmf_cuda_batch_run(cdmf_batch* B, int n_outer, double* rmse_out) {
                 for (int o = 0; o < n_outer; ++o) rmse_out[(size_t)q * n_outer + o] = -1.0;
             }
         }
+    if (B->st.nonfinite) return bfail(B, CDMF_ERR_NUMERIC, "non-finite residual values at a refresh");
     return CDMF_OK;
 }
 

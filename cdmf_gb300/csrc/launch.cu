@@ -166,55 +166,12 @@ void blocked_rt(const BlockedArgs& B, int mode, bool sub, bool add, unsigned gri
     else blocked_mode<RT, M_PLAIN>(B, false, false, grid, s);
 }
 
-template <int RT>
-void grouped_rt(int mode, bool sub, bool add, const SweepArgs* d, const uint32_t* pre, uint32_t nq, uint32_t* queue,
-                int grid, cudaStream_t s) {
-    prefer_l1(grouped_sweep_kernel<RT, M_CSC, true, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR, true, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSC, true, false>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR, true, false>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSC, false, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR, false, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_PLAIN, false, false>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR16, true, true>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR16, true, false>);
-    prefer_l1(grouped_sweep_kernel<RT, M_CSR16, false, true>);
-#define CDMF_G(M, S, A) grouped_sweep_kernel<RT, M, S, A><<<grid, kBlock, 0, s>>>(d, pre, nq, queue)
-    if (mode == M_PLAIN) CDMF_G(M_PLAIN, false, false);
-    else if (mode == M_CSC) {
-        if (sub && add) CDMF_G(M_CSC, true, true);
-        else if (sub) CDMF_G(M_CSC, true, false);
-        else if (add) CDMF_G(M_CSC, false, true);
-        else CDMF_G(M_CSC, false, false);
-    } else if (mode == M_CSR16) {
-        if (sub && add) CDMF_G(M_CSR16, true, true);
-        else if (sub) CDMF_G(M_CSR16, true, false);
-        else if (add) CDMF_G(M_CSR16, false, true);
-        else CDMF_G(M_CSR16, false, false);
-    } else {
-        if (sub && add) CDMF_G(M_CSR, true, true);
-        else if (sub) CDMF_G(M_CSR, true, false);
-        else if (add) CDMF_G(M_CSR, false, true);
-        else CDMF_G(M_CSR, false, false);
-    }
-#undef CDMF_G
-}
-
 #define CDMF_INST(RT)                                                                                  \
     template void tile_rt<RT>(const TileArgs&, int, bool, bool, unsigned, cudaStream_t);                \
-    template void blocked_rt<RT>(const BlockedArgs&, int, bool, bool, unsigned, cudaStream_t);          \
-    template void grouped_rt<RT>(int, bool, bool, const SweepArgs*, const uint32_t*, uint32_t, uint32_t*, int, \
-                                 cudaStream_t);
+    template void blocked_rt<RT>(const BlockedArgs&, int, bool, bool, unsigned, cudaStream_t);
 CDMF_FOR_RT(CDMF_INST)
 #undef CDMF_INST
 
-#if CDMF_HAS_RT0
-int grouped_blocks_per_sm() {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_sweep_kernel<0, M_CSR, true, true>, kBlock, 0);
-    return per_sm;
-}
-#endif
 
 template <int RT>
 void launch_refresh_rt(const RefreshDesc& D, unsigned grid, cudaStream_t s) {

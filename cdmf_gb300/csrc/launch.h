@@ -72,7 +72,7 @@ void smemq_rt(const SweepArgs& A, bool i16, bool sub, bool add, unsigned grid, s
 // The dual SpMV (M_DUAL, FP32 values only).
 void launch_dual(const SweepArgs& A, unsigned grid, cudaStream_t s);
 
-// --- family 1 (launch.cu, CDMF_LAUNCH_PART 1): tiles, blocks, batches, refresh ---
+// --- family 1 (launch.cu, CDMF_LAUNCH_PART 1): tiles, blocks, refresh ---
 
 // tile_sweep_kernel (nonzero-balanced tiles); mode M_PLAIN, M_CSC or M_CSR.
 template <int RT>
@@ -81,15 +81,6 @@ void tile_rt(const TileArgs& T, int mode, bool sub, bool add, unsigned grid, cud
 // blocked_sweep_kernel (cross table blocks in shared memory).
 template <int RT>
 void blocked_rt(const BlockedArgs& B, int mode, bool sub, bool add, unsigned grid, cudaStream_t s);
-
-// grouped_sweep_kernel: one sweep of many problems over a work queue.
-template <int RT>
-void grouped_rt(int mode, bool sub, bool add, const SweepArgs* d, const uint32_t* pre, uint32_t nq, uint32_t* queue,
-                int grid, cudaStream_t s);
-
-// Resident blocks per SM of the grouped sweep (FP32, first CSR sweep): the
-// persistent grid of a batch is this times the SM count.
-int grouped_blocks_per_sm();
 
 // refresh_warp_kernel over one problem; D.slices picks the instantiation
 // (1, 2, 4, 8 slices of the rank, 0 = any rank).  RT is 1 or 2.

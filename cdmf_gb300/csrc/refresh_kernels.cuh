@@ -207,8 +207,7 @@ __global__ void __launch_bounds__(kBlock) refresh_warp_kernel(
                         drift_out, nonfinite_out, blockIdx.x, gridDim.x);
 }
 
-// The refreshes of many problems (one residual type) in one launch, and the
-// row-major factor copies they read, also in one launch.
+// One refresh's arguments (launch_refresh_rt).
 struct RefreshDesc {
     const uint32_t *ptr, *idx;
     const float* val;
@@ -223,55 +222,5 @@ struct RefreshDesc {
     double* drift_out;
     unsigned long long* nonfinite;
 };
-
-template <int RT>
-__global__ void __launch_bounds__(kBlock) grouped_refresh_kernel(const RefreshDesc* __restrict__ descs,
-                                                                 const uint32_t* __restrict__ prefix, uint32_t nprob) {
-    const uint32_t q = group_of(prefix, nprob, blockIdx.x);
-    const RefreshDesc D = descs[q];
-    const uint32_t b = blockIdx.x - prefix[q], nb = prefix[q + 1] - prefix[q];
-#define CDMF_REFRESH_CASE(SS)                                                                                     \
-    refresh_body<RT, SS>(D.ptr, D.idx, D.val, D.to_csr, D.to_csc, D.m, D.nnz, D.Wrm, D.Hrm, D.kp, D.res_csr,      \
-                         D.res_csc, D.pa, D.pb, D.part, D.counter, D.drift_out, D.nonfinite, b, nb)
-    switch (D.slices) {
-        case 1: CDMF_REFRESH_CASE(1); break;
-        case 2: CDMF_REFRESH_CASE(2); break;
-        case 4: CDMF_REFRESH_CASE(4); break;
-        case 8: CDMF_REFRESH_CASE(8); break;
-        default: CDMF_REFRESH_CASE(0); break;
-    }
-#undef CDMF_REFRESH_CASE
-}
-
-struct TransposeDesc {
-    const float* X;     // k x len, feature-major
-    float* Y;           // len x kp, row-major
-    uint32_t k, kp;
-    int64_t len;
-    uint32_t tiles_x;   // 32-row tiles
-};
-
-static __global__ void __launch_bounds__(kBlock) grouped_row_major_kernel(const TransposeDesc* __restrict__ descs,
-                                                                   const uint32_t* __restrict__ prefix,
-                                                                   uint32_t nprob) {
-    __shared__ float tile[32][33];
-    const uint32_t q = group_of(prefix, nprob, blockIdx.x);
-    const TransposeDesc D = descs[q];
-    const uint32_t b = blockIdx.x - prefix[q];
-    const int64_t i0 = (int64_t)(b % D.tiles_x) * 32;
-    const uint32_t t0 = (b / D.tiles_x) * 32;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int r = ty; r < 32; r += 8) {
-        const uint32_t t = t0 + r;
-        const int64_t i = i0 + tx;
-        tile[r][tx] = (t < D.k && i < D.len) ? D.X[(size_t)t * D.len + i] : 0.0f;
-    }
-    __syncthreads();
-    for (int r = ty; r < 32; r += 8) {
-        const int64_t i = i0 + r;
-        const uint32_t t = t0 + tx;
-        if (i < D.len && t < D.kp) D.Y[(size_t)i * D.kp + t] = tile[tx][r];
-    }
-}
 
 }  // namespace cdmf

@@ -617,30 +617,6 @@ __global__ void __launch_bounds__(kBlock * kSubs, 1) sweep_smemq_kernel(const Sw
     }
 }
 
-// Many problems' sweeps in one persistent launch: resident blocks pull block
-// indices from a device work queue (an atomic counter) over the concatenated
-// block ranges of all problems; prefix[q] is problem q's first block.
-template <int RT, int MODE, bool SUB, bool ADD>
-__global__ void CDMF_SWEEP_BOUNDS grouped_sweep_kernel(const SweepArgs* __restrict__ descs,
-                                                       const uint32_t* __restrict__ prefix, uint32_t nprob,
-                                                       uint32_t* queue) {
-    __shared__ uint32_t blk;
-    const uint32_t total = prefix[nprob];
-    for (;;) {
-        if (threadIdx.x == 0) blk = atomicAdd(queue, 1u);
-        __syncthreads();
-        const uint32_t b = blk;
-        __syncthreads();
-        if (b >= total) return;
-        uint32_t lo = 0, hi = nprob;                       // last q with prefix[q] <= b
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (prefix[mid] <= b) lo = mid; else hi = mid;
-        }
-        sweep_block<RT, MODE, SUB, ADD>(descs[lo], b - prefix[lo]);
-    }
-}
-
 // P[i] = (prev[i] or 0, cur[i]): the packed CSC table when no sweep has
 // written it (start of a run, after a state change).
 static __global__ void pack_p_kernel(float2* __restrict__ P, const float* __restrict__ prev, const float* __restrict__ cur,
@@ -730,37 +706,6 @@ __global__ void __launch_bounds__(kBlock) rmse_kernel(const uint32_t* __restrict
                                                       uint32_t* counter, double* out,
                                                       unsigned long long* nan_out) {
     rmse_body<VT>(row, col, val, nt, W, H, m, n, k, part, counter, out, nan_out, blockIdx.x, gridDim.x);
-}
-
-// Block index b of a grouped launch over nprob problems whose block ranges
-// are concatenated: the problem q with prefix[q] <= b < prefix[q + 1].
-__device__ __forceinline__ uint32_t group_of(const uint32_t* __restrict__ prefix, uint32_t nprob, uint32_t b) {
-    uint32_t lo = 0, hi = nprob;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (prefix[mid] <= b) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
-// Test RMSE of many problems in one launch.
-struct RmseDesc {
-    const uint32_t *row, *col;
-    const float* val;
-    int64_t nt, m, n;
-    const float *W, *H;
-    uint32_t k;
-    double* part;
-    uint32_t* counter;
-    double* out;
-};
-
-static __global__ void __launch_bounds__(kBlock) grouped_rmse_kernel(const RmseDesc* __restrict__ descs,
-                                                              const uint32_t* __restrict__ prefix, uint32_t nprob) {
-    const uint32_t q = group_of(prefix, nprob, blockIdx.x);
-    const RmseDesc D = descs[q];
-    rmse_body<float>(D.row, D.col, D.val, D.nt, D.W, D.H, D.m, D.n, D.k, D.part, D.counter, D.out, nullptr,
-                     blockIdx.x - prefix[q], prefix[q + 1] - prefix[q]);
 }
 
 }  // namespace cdmf

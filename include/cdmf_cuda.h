@@ -263,22 +263,25 @@ int cdmf_cuda_bins(const cdmf_handle* h, int which, int64_t counts[5], int64_t n
 
 /* ---- Batches of independent factorisations --------------------------------
  * No counterpart in the reference (which runs one problem per process).
- * nprob problems of uneven sizes, each with its own k and lambda, advance in
- * lockstep: at feature index t the sweeps of every problem with k > t run in
- * one persistent launch whose resident blocks pull (problem, bin-block) work
- * from a device queue; with opts[0].use_graph the whole run is replayed as
- * one CUDA graph.  All problems must share device, residual, reduce and
- * maxinneriter.  W0/W/H are arrays of nprob pointers (k_q x m_q, k_q x n_q).
- * rmse_out holds nprob x n_outer values (problem-major). */
+ * nprob problems of uneven sizes, each with its own k and lambda, each run by
+ * its own engine on its own CUDA stream with its single-problem schedule; a
+ * batched run issues all problems' outer iterations together so that the GPU
+ * overlaps their kernels, and with opts[0].use_graph it is captured once as
+ * one CUDA graph (a branch per problem) and replayed after.  Results are
+ * bit-identical to running each problem alone.  All problems must share
+ * device, residual, reduce and maxinneriter.  W0/W/H are arrays of nprob
+ * pointers (k_q x m_q, k_q x n_q).  rmse_out holds nprob x n_outer values
+ * (problem-major). */
 typedef struct cdmf_batch cdmf_batch;
 int cdmf_cuda_batch_create(const cdmf_problem* probs, const cdmf_opts* opts, int nprob, cdmf_batch** out);
 void cdmf_cuda_batch_destroy(cdmf_batch* b);
 const char* cdmf_cuda_batch_last_error(const cdmf_batch* b);
 int cdmf_cuda_batch_set_factors(cdmf_batch* b, const float* const* W0);
 int cdmf_cuda_batch_run(cdmf_batch* b, int n_outer, double* rmse_out);
-/* The same problems run one after another through their own handles (the
- * per-problem launch schedule), timed on the batch stream: the comparison
- * point for cdmf_cuda_batch_run. */
+/* The same problems run one after another through their own handles (each
+ * run finished before the next starts, launches issued eagerly), timed on the
+ * host clock of the batch stream: the comparison point for
+ * cdmf_cuda_batch_run. */
 int cdmf_cuda_batch_run_sequential(cdmf_batch* b, int n_outer, double* rmse_out, double* ms_out);
 int cdmf_cuda_batch_get_factors(cdmf_batch* b, float* const* W, float* const* H);
 int cdmf_cuda_batch_stats(const cdmf_batch* b, cdmf_stats* s);
