@@ -224,6 +224,7 @@ struct cdmf_handle {
     float *Wrm = nullptr, *Hrm = nullptr;
     uint32_t kp = 0;
     int ref_grid = 0;
+    uint32_t* ref_crow = nullptr;    // refresh: row of each chunk's first nonzero, then of the last one
     double *ref_part = nullptr, *drift_out = nullptr;
     uint32_t* ref_count = nullptr;
     unsigned long long* nonfinite = nullptr;
@@ -706,6 +707,7 @@ int flush_pending(cdmf_handle* h) {
 void launch_refresh(cdmf_handle* h, int rt, int nu, const float* pa, const float* pb) {
     RefreshDesc D;
     D.ptr = h->csr_ptr;
+    D.crow = h->ref_crow;
     D.idx = h->csr_idx;
     D.val = h->csr_val;
     D.to_csr = h->ref_to_csr;
@@ -1260,6 +1262,18 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if ((r = upload_bins(h, h->csr, plan_bins(h->hptr_r.data(), m, seq, h->cfg))) ||
         (r = upload_bins(h, h->csc, plan_bins(h->hptr_c.data(), n, seq, h->cfg))))
         return bail(r);
+    if (h->rt != 0 && N > 0) {
+        // the refresh's chunk start rows: the row holding nonzero c * kRefreshChunk, then the last row
+        const int64_t nch = (N + kRefreshChunk - 1) / kRefreshChunk;
+        std::vector<uint32_t> crow(nch + 1);
+        for (int64_t c = 0; c <= nch; ++c) {
+            const uint32_t pos = (uint32_t)std::min<int64_t>(c * kRefreshChunk, N - 1);
+            crow[c] = (uint32_t)(std::upper_bound(h->hptr_r.begin(), h->hptr_r.end(), pos) - h->hptr_r.begin() - 1);
+        }
+        if ((r = dalloc(h, &h->ref_crow, nch + 1)) || (r = up(h->ref_crow, crow.data(), 4 * (nch + 1))))
+            return bail(r);
+        if (cudaStreamSynchronize(h->s) != cudaSuccess) return bail(CDMF_ERR_CUDA);
+    }
     phase("bins");
     h->tiles = o->version == 3 && !seq && !h->blocked;
     if (h->tiles && ((r = upload_tiles(h, h->tcsr, h->hptr_r.data(), m, N)) ||

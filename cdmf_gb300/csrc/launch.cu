@@ -145,8 +145,8 @@ void blocked_mode(const BlockedArgs& B, bool sub, bool add, unsigned grid, cudaS
 
 template <int RT, int NU>
 void refresh_t(const RefreshDesc& D, unsigned grid, cudaStream_t s) {
-    refresh_warp_kernel<RT, NU><<<grid, kBlock, 0, s>>>(D.ptr, D.idx, D.val, D.to_csr, D.to_csc, D.m, D.nnz, D.Wrm,
-                                                        D.Hrm, D.kp, D.res_csr, D.res_csc, D.pa, D.pb, D.part,
+    refresh_warp_kernel<RT, NU><<<grid, kBlock, 0, s>>>(D.ptr, D.crow, D.idx, D.val, D.to_csr, D.to_csc, D.nnz,
+                                                        D.Wrm, D.Hrm, D.kp, D.res_csr, D.res_csc, D.pa, D.pb, D.part,
                                                         D.counter, D.drift_out, D.nonfinite);
 }
 

@@ -57,15 +57,17 @@ static __global__ void __launch_bounds__(kBlock) to_row_major_kernel(const float
 // k.  Products are summed in a fixed order: deterministic.
 constexpr int kRefG = 4;
 
-// Block `bid` of `nblk` blocks of one refresh.
+// Block `bid` of `nblk` blocks of one refresh.  crow[c] is the row holding
+// the chunk's first nonzero c * kRefreshChunk, and crow[nchunks] the row of
+// the last nonzero (built at create), so a lane's row search starts inside
+// the chunk's few rows.
 template <int RT, int S>
 __device__ __forceinline__ void refresh_body(
-    const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ idx, const float* __restrict__ val,
-    const uint32_t* __restrict__ to_csr, const uint32_t* __restrict__ to_csc, int64_t m, int64_t nnz,
-    const float* __restrict__ Wrm, const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr,
+    const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ crow, const uint32_t* __restrict__ idx,
+    const float* __restrict__ val, const uint32_t* __restrict__ to_csr, const uint32_t* __restrict__ to_csc,
+    int64_t nnz, const float* __restrict__ Wrm, const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr,
     void* __restrict__ res_csc, const float* __restrict__ pa, const float* __restrict__ pb_, double* part,
     uint32_t* counter, double* drift_out, unsigned long long* nonfinite_out, uint32_t bid, uint32_t nblk) {
-    __shared__ uint32_t srow[2];
     constexpr unsigned FULL = 0xffffffffu;
     constexpr int kPer = 32 / kRefG;   // nonzeros per round
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -78,17 +80,7 @@ __device__ __forceinline__ void refresh_body(
     for (int64_t c = bid; c < nchunks; c += nblk) {
         const int64_t p0 = c * kRefreshChunk;
         const int64_t p1 = (p0 + kRefreshChunk < nnz) ? p0 + kRefreshChunk : nnz;
-        if (threadIdx.x < 2) {
-            const int64_t p = threadIdx.x == 0 ? p0 : p1 - 1;
-            int64_t lo = 0, hi = m;   // ptr[lo] <= p < ptr[hi]
-            while (hi - lo > 1) {
-                const int64_t mid = (lo + hi) >> 1;
-                if ((int64_t)ptr[mid] <= p) lo = mid; else hi = mid;
-            }
-            srow[threadIdx.x] = (uint32_t)lo;
-        }
-        __syncthreads();
-        const uint32_t rlo = srow[0], rhi = srow[1];
+        const uint32_t rlo = __ldg(crow + c), rhi = __ldg(crow + c + 1);
         float dsq = 0.0f;   // this chunk's squared drift (at most kRefreshPerThread terms per lane)
         for (int s = 0; s < kRefreshPerThread; ++s) {
             const int64_t base = p0 + ((int64_t)warp * kRefreshPerThread + s) * 32;
@@ -162,7 +154,6 @@ __device__ __forceinline__ void refresh_body(
             }
         }
         drift = __dadd_rn(drift, (double)dsq);
-        __syncthreads();
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -198,18 +189,18 @@ __device__ __forceinline__ void refresh_body(
 
 template <int RT, int S>
 __global__ void __launch_bounds__(kBlock) refresh_warp_kernel(
-    const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ idx, const float* __restrict__ val,
-    const uint32_t* __restrict__ to_csr, const uint32_t* __restrict__ to_csc, int64_t m, int64_t nnz,
-    const float* __restrict__ Wrm, const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr,
+    const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ crow, const uint32_t* __restrict__ idx,
+    const float* __restrict__ val, const uint32_t* __restrict__ to_csr, const uint32_t* __restrict__ to_csc,
+    int64_t nnz, const float* __restrict__ Wrm, const float* __restrict__ Hrm, uint32_t kp, void* __restrict__ res_csr,
     void* __restrict__ res_csc, const float* __restrict__ pa, const float* __restrict__ pb_, double* part,
     uint32_t* counter, double* drift_out, unsigned long long* nonfinite_out) {
-    refresh_body<RT, S>(ptr, idx, val, to_csr, to_csc, m, nnz, Wrm, Hrm, kp, res_csr, res_csc, pa, pb_, part, counter,
-                        drift_out, nonfinite_out, blockIdx.x, gridDim.x);
+    refresh_body<RT, S>(ptr, crow, idx, val, to_csr, to_csc, nnz, Wrm, Hrm, kp, res_csr, res_csc, pa, pb_, part,
+                        counter, drift_out, nonfinite_out, blockIdx.x, gridDim.x);
 }
 
 // One refresh's arguments (launch_refresh_rt).
 struct RefreshDesc {
-    const uint32_t *ptr, *idx;
+    const uint32_t *ptr, *crow, *idx;
     const float* val;
     const uint32_t *to_csr, *to_csc;
     int64_t m, nnz;
