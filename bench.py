@@ -376,9 +376,9 @@ def main():
 
 def measure_batch(args, threads, residual):
     """64 independent problems (sizes, k and lambda drawn per problem, 10 x 1):
-    one batched run (grouped persistent sweeps, one CUDA graph) against the
-    same problems run one after another through their own handles.  Returns
-    the batch's measurement as a dict."""
+    one batched run (each problem's launches on its own stream, the whole run
+    one CUDA graph) against the same problems run one after another through
+    their own handles.  Returns the batch's measurement as a dict."""
     from cdmf_gb300 import engine, synth
     specs = synth.batch_specs(64, seed=0)
     probs = [synth.generate(threads=threads, **sp["matrix"]) for sp in specs]
