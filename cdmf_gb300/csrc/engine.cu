@@ -552,6 +552,7 @@ int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A,
     const unsigned grid = D.nx + D.nc + D.nwb + D.ngb + D.ntb;
     if (grid == 0) return CDMF_OK;
     if (mode == M_CSR && h->idx16) mode = M_CSR16;
+    if (mode == M_CSC && h->nnz >= kLargeNnz) mode = M_CSCP;
     {
         Timed tm(h, kind);
         switch (h->rt) {

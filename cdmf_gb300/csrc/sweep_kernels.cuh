@@ -42,15 +42,12 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace cdmf {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
-// Resident blocks per SM asked of the compiler (register cap): 6 blocks of
-// 256 threads (at most 40 registers) measured best on the 480,189 x 17,770
-// workload, against 4 and 5 blocks with more chunks in flight per lane.
-constexpr int kSweepBlocks = 6;
-#define CDMF_SWEEP_BOUNDS __launch_bounds__(kBlock, kSweepBlocks)
 constexpr int kTileBlocks = 6;
 
 // sweep modes
@@ -61,9 +58,27 @@ constexpr int M_DUAL = 3;   // dual SpMV (CSR5-style front end): y gathers, raw 
 constexpr int M_CSRS = 4;   // M_CSR with the cross table staged in shared memory (narrow matrices)
 constexpr int M_CSR16 = 5;  // M_CSR reading 16-bit column indices (at most 65,536 columns)
 constexpr int M_CSRS16 = 6; // M_CSRS reading 16-bit column indices
+constexpr int M_CSCP = 7;   // M_CSC, software-pipelined at 4 blocks per SM (large matrices)
 template <int MODE> constexpr bool kIdx16 = MODE == M_CSR16 || MODE == M_CSRS16;
 template <int MODE> constexpr bool kCsrFirst = MODE == M_CSR || MODE == M_CSR16;
 template <int MODE> constexpr bool kCsrShared = MODE == M_CSRS || MODE == M_CSRS16;
+template <int MODE> constexpr bool kCscFirst = MODE == M_CSC || MODE == M_CSCP;
+
+// Resident blocks per SM asked of the compiler (register cap) and the
+// software-pipeline depth of the vector layout, per sweep mode.  Measured on
+// the 480,189 x 17,770 workload (BF16 / FP32 residual, us per launch):
+//   CSC sweep: 6 blocks, no pipeline 223 / 269; M_CSCP, 4 blocks (56
+//              registers), streams of the next 2 chunks loaded before the
+//              gathers of the current 2: 200 / 251; 3 blocks 200; 5 blocks
+//              205; 1 or 3 chunks at 4 blocks 213 / 201.
+//   CSR sweeps: 6 blocks, no pipeline 216; 5 blocks 220; 4 blocks, 2 chunks
+//              231; 6 blocks with a pipeline spill (40 registers): 411.  They
+//              are bound by L1 data-pipe wavefronts (81 % of peak), not by
+//              latency.
+// On the 64-problem batch (short lines) M_CSCP measured 5 % slower than
+// M_CSC, so the engine takes it from 16M nonzeros up.
+template <int MODE> constexpr int kSweepBlocks = MODE == M_CSCP ? 4 : 6;
+template <int MODE> constexpr int kPipe = MODE == M_CSCP ? 2 : 0;
 
 struct XTask {            // one chunk of a split line
     uint32_t line, beg, end, slot;
@@ -232,7 +247,7 @@ template <bool KAHAN> struct Acc {
 // Cross-vector values of one nonzero with cross index i.
 template <int MODE>
 __device__ __forceinline__ void fetch(const SweepArgs& A, uint32_t i, float& a, float& c, float& y) {
-    if (MODE == M_CSC) {
+    if (kCscFirst<MODE>) {
         const float2 p = __ldg(A.P + i);
         a = p.x;
         c = p.y;
@@ -300,9 +315,61 @@ __device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, 
 constexpr int kChunks = 2;   // vector layout: 4-element chunks in flight per lane
 constexpr int kIlp = 4;      // interleaved layout: elements in flight per lane
 
-// Vector layout (default; measured faster for 16-bit residuals): lane takes 4 consecutive nonzeros per 128-bit load, after a
-// scalar head that reaches a 4-aligned position, then a scalar tail.
-template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
+// Packed stream values of one 4-element chunk, index (4 x 32-bit or 4 x
+// 16-bit) and residual (4 x FP32 or 4 x 16-bit), held packed while in flight.
+template <int RT, int MODE>
+struct Chunk4 {
+    using IT = typename std::conditional<kIdx16<MODE>, uint2, uint4>::type;
+    using VT = typename std::conditional<RT == 0, uint4, uint2>::type;
+    IT i;
+    VT r;
+    __device__ __forceinline__ void load(const SweepArgs& A, uint32_t q) {
+        if constexpr (kIdx16<MODE>) i = ld_stream2(A.idx16 + q);
+        else i = ld_stream4(A.idx + q);
+        if constexpr (RT == 0) r = ld_stream4((const float*)A.res + q);
+        else r = ld_stream2((const unsigned short*)A.res + q);
+    }
+    __device__ __forceinline__ uint32_t idx(int e) const {
+        if constexpr (kIdx16<MODE>) {
+            const uint32_t w = e < 2 ? i.x : i.y;
+            return (e & 1) ? (w >> 16) : (w & 0xffffu);
+        } else {
+            return e == 0 ? i.x : e == 1 ? i.y : e == 2 ? i.z : i.w;
+        }
+    }
+    __device__ __forceinline__ float res(int e) const {
+        if constexpr (RT == 0) {
+            return __uint_as_float(e == 0 ? r.x : e == 1 ? r.y : e == 2 ? r.z : r.w);
+        } else {
+            const uint32_t w = e < 2 ? r.x : r.y;
+            return Res16<RT>::to_f((unsigned short)((e & 1) ? (w >> 16) : (w & 0xffffu)));
+        }
+    }
+};
+
+// Update, store and accumulate the 4 elements of a loaded chunk at q.
+template <int RT, int MODE, bool SUB, bool ADD, class AccT>
+__device__ __forceinline__ void chunk4(const SweepArgs& A, uint32_t q, const Chunk4<RT, MODE>& C, float bj, float dj,
+                                       AccT& g, AccT& h) {
+    float r[4], y[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float a, c;
+        fetch<MODE>(A, C.idx(e), a, c, y[e]);
+        r[e] = update<SUB, ADD>(C.res(e), a, c, bj, dj);
+    }
+    if (SUB || ADD) Res<RT>::st4(A.res, q, r);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) accumulate(g, h, y[e], r[e]);
+}
+
+// Vector layout (default; measured faster for 16-bit residuals): lane takes
+// 4 consecutive nonzeros per 128-bit load, after a scalar head that reaches a
+// 4-aligned position, then a scalar tail.  PIPE = 0: kChunks chunks loaded,
+// then their gathers; PIPE > 0: software-pipelined, the streams of the next
+// PIPE chunks are loaded before the gathers of the current PIPE chunks.  Both
+// visit a lane's elements in increasing order, so their sums are identical.
+template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN, int PIPE>
 __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
                                             float dj, float& gs, float& hs) {
     Acc<KAHAN> g, h;
@@ -311,6 +378,30 @@ __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, ui
     const uint32_t vend = vbeg + ((end - vbeg) & ~3u);
     if (lane < vbeg - beg) elem1<RT, MODE, SUB, ADD>(A, beg + lane, bj, dj, g, h);
     uint32_t q = vbeg + 4u * lane;
+    if constexpr (PIPE > 0) {
+        constexpr uint32_t STEP = 4u * S;
+        if (q < vend) {
+            Chunk4<RT, MODE> cur[PIPE];
+#pragma unroll
+            for (int u = 0; u < PIPE; ++u)
+                if (q + u * STEP < vend) cur[u].load(A, q + u * STEP);
+            for (;;) {
+                const uint32_t qn = q + PIPE * STEP;
+                Chunk4<RT, MODE> nxt[PIPE];
+#pragma unroll
+                for (int u = 0; u < PIPE; ++u)
+                    if (qn + u * STEP < vend) nxt[u].load(A, qn + u * STEP);
+#pragma unroll
+                for (int u = 0; u < PIPE; ++u)
+                    if (q + u * STEP < vend) chunk4<RT, MODE, SUB, ADD>(A, q + u * STEP, cur[u], bj, dj, g, h);
+                if (qn >= vend) break;
+                q = qn;
+#pragma unroll
+                for (int u = 0; u < PIPE; ++u) cur[u] = nxt[u];
+            }
+        }
+        q = vend;
+    }
     for (; q + 4u * S * (kChunks - 1) < vend; q += 4u * S * kChunks) {
         uint32_t iv[kChunks][4];
         float r[kChunks][4];
@@ -398,7 +489,7 @@ __device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32
     if (S <= 8 && end - beg <= A.group_short)
         strided_il<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
     else
-        strided_vec<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
+        strided_vec<RT, MODE, SUB, ADD, S, KAHAN, kPipe<MODE>>(A, beg, end, lane, bj, dj, gs, hs);
 }
 
 template <int WIDTH = 32>
@@ -431,7 +522,7 @@ __device__ __forceinline__ void cta_sum2(float& g, float& h) {
 template <int MODE>
 __device__ __forceinline__ void write_line(const SweepArgs& A, uint32_t j, float x, float bj, float dj) {
     A.out[j] = x;
-    if (MODE == M_CSC) A.emitQ[j] = make_float4(bj, dj, x, 0.0f);
+    if (kCscFirst<MODE>) A.emitQ[j] = make_float4(bj, dj, x, 0.0f);
     if (A.emitP) A.emitP[j] = make_float2(x, A.next_old == A.out ? x : A.next_old[j]);
 }
 
@@ -452,8 +543,8 @@ __device__ __forceinline__ void finish_line(const SweepArgs& A, uint32_t j, uint
 // feature's old value).  The CSC sweep also forwards them into Q.
 template <int MODE, bool SUB, bool ADD>
 __device__ __forceinline__ void line_scalars(const SweepArgs& A, uint32_t j, float& bj, float& dj) {
-    bj = (SUB || MODE == M_CSC) && A.b ? A.b[j] : 0.0f;
-    dj = (ADD || MODE == M_CSC) ? A.d[j] : 0.0f;
+    bj = (SUB || kCscFirst<MODE>) && A.b ? A.b[j] : 0.0f;
+    dj = (ADD || kCscFirst<MODE>) ? A.d[j] : 0.0f;
 }
 
 // Block b of the group bin: one line per L-lane group, kBlock / L lines.
@@ -585,7 +676,7 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
 }
 
 template <int RT, int MODE, bool SUB, bool ADD>
-__global__ void CDMF_SWEEP_BOUNDS sweep_kernel(const SweepArgs A) {
+__global__ void __launch_bounds__(kBlock, kSweepBlocks<MODE>) sweep_kernel(const SweepArgs A) {
     sweep_block<RT, MODE, SUB, ADD>(A, blockIdx.x);
 }
 
