@@ -212,6 +212,11 @@ struct cdmf_handle {
     uint32_t group_lanes = 8;        // lanes per group-bin line (4 on large matrices)
     uint16_t* csr_idx16 = nullptr;   // narrow matrices: the CSR column indices in 16 bits
     bool idx16 = false;
+    // large matrices with fewer than 2^19 rows: the CSC row indices as 16-bit
+    // offsets inside segments of 65,536 rows, and each column's run ends
+    uint16_t* csc_idx16 = nullptr;
+    uint32_t* csc_seg = nullptr;
+    bool cidx16 = false;
     bool smemq = false;
     int sms = 0;
     uint32_t* smemq_queue = nullptr;
@@ -552,7 +557,7 @@ int launch_sweep(cdmf_handle* h, int kind, const DevBins& D, const SweepArgs& A,
     const unsigned grid = D.nx + D.nc + D.nwb + D.ngb + D.ntb;
     if (grid == 0) return CDMF_OK;
     if (mode == M_CSR && h->idx16) mode = M_CSR16;
-    if (mode == M_CSC && h->nnz >= kLargeNnz) mode = M_CSCP;
+    if (mode == M_CSC && h->nnz >= kLargeNnz) mode = h->cidx16 ? M_CSCQ : M_CSCP;
     {
         Timed tm(h, kind);
         switch (h->rt) {
@@ -587,6 +592,8 @@ void feature_args(cdmf_handle* h, uint32_t t, int it, SweepArgs& A, SweepArgs& B
         A.b = Hp;
         A.d = Ht;
         A.emitQ = h->Q;
+        A.idx16 = h->csc_idx16;
+        A.cseg = h->csc_seg;
     } else {
         A.y = Wt;
     }
@@ -787,6 +794,27 @@ int factors_out(cdmf_handle* h, const float* dev, float* user, int64_t len, cons
 __global__ void narrow_idx_kernel(const uint32_t* __restrict__ src, uint16_t* __restrict__ dst, int64_t count) {
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x)
         dst[q] = (uint16_t)src[q];
+}
+
+// cseg[kCSeg * j + h]: the end of run h of column j, i.e. the first position
+// of the column whose row is at least (h + 1) * 65,536 (the column's end for
+// h = kCSeg - 1).  One thread per (column, run); rows ascend in a column.
+__global__ void csc_segments_kernel(const uint32_t* __restrict__ ptr, const uint32_t* __restrict__ idx, int64_t n,
+                                    uint32_t* __restrict__ seg) {
+    const int64_t total = n * kCSeg;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = t / kCSeg;
+        const uint32_t h = (uint32_t)(t % kCSeg);
+        uint32_t lo = ptr[j], hi = ptr[j + 1];
+        if (h + 1 < kCSeg) {
+            const uint32_t bound = (h + 1) << 16;
+            while (lo < hi) {   // first position with row >= bound
+                const uint32_t mid = lo + (hi - lo) / 2;
+                if (idx[mid] < bound) lo = mid + 1; else hi = mid;
+            }
+        }
+        seg[t] = lo;
+    }
 }
 
 __global__ void f32_to_res_kernel(const float* __restrict__ src, void* __restrict__ dst, int64_t count, int rt) {
@@ -1296,6 +1324,17 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         if (cudaGetLastError() != cudaSuccess) return bail(CDMF_ERR_CUDA);
         h->idx16 = true;
     }
+    // large matrices (the pipelined CSC sweep) with fewer than kCSeg * 65,536
+    // rows: the first CSC sweep of each feature streams 16-bit row offsets
+    if (!seq && !h->blocked && !h->tiles && N >= kLargeNnz && m <= (int64_t)kCSeg << 16 &&
+        !std::getenv("CDMF_NO_IDX16")) {
+        if ((r = dalloc(h, &h->csc_idx16, N)) || (r = dalloc(h, &h->csc_seg, (size_t)n * kCSeg))) return bail(r);
+        narrow_idx_kernel<<<1216, kBlock, 0, h->s>>>(h->csc_idx, h->csc_idx16, N);
+        csc_segments_kernel<<<(unsigned)std::min<int64_t>(4096, (n * kCSeg + kBlock - 1) / kBlock), kBlock, 0, h->s>>>(
+            h->csc_ptr, h->csc_idx, n, h->csc_seg);
+        if (cudaGetLastError() != cudaSuccess) return bail(CDMF_ERR_CUDA);
+        h->cidx16 = true;
+    }
     // fresh state: W := 0 until set, H := 0, residual := ratings
     if (cudaMemsetAsync(h->W, 0, sizeof(float) * k * m, h->s) != cudaSuccess ||
         cudaMemsetAsync(h->H, 0, sizeof(float) * k * n, h->s) != cudaSuccess)
@@ -1308,10 +1347,12 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     const double T = std::max(1, o->maxinneriter);
     const double br = (double)h->rbytes;
     const double bi = h->blocked ? 2.0 : 4.0;   // index bytes as stored
-    // the first CSR sweep of a feature reads 16-bit indices when idx16 is on
+    // the first CSR (CSC) sweep of a feature reads 16-bit indices when idx16
+    // (cidx16) is on
     const double bi_csr1 = h->idx16 ? 2.0 : bi;
-    h->st.bytes_per_update = T * N * (bi + br) + N * (bi_csr1 + br) + (T - 1) * N * (bi + br) + 2.0 * N * br +
-                             T * 4.0 * (m + n + 2) + 8.0 * (m + n);
+    const double bi_csc1 = h->cidx16 ? 2.0 : bi;
+    h->st.bytes_per_update = N * (bi_csc1 + br) + (T - 1) * N * (bi + br) + N * (bi_csr1 + br) +
+                             (T - 1) * N * (bi + br) + 2.0 * N * br + T * 4.0 * (m + n + 2) + 8.0 * (m + n);
     *out = h;
     return CDMF_OK;
 }

@@ -76,6 +76,7 @@ template <int RT>
 void launch_rt(const SweepArgs& A, int mode, bool sub, bool add, unsigned grid, cudaStream_t s) {
     if (mode == M_CSC) launch_mode<RT, M_CSC>(A, sub, add, grid, s);
     else if (mode == M_CSCP) launch_mode<RT, M_CSCP>(A, sub, add, grid, s);
+    else if (mode == M_CSCQ) launch_mode<RT, M_CSCQ>(A, sub, add, grid, s);
     else if (mode == M_CSR) launch_mode<RT, M_CSR>(A, sub, add, grid, s);
     else if (mode == M_CSR16) launch_mode<RT, M_CSR16>(A, sub, add, grid, s);
     else launch_mode<RT, M_PLAIN>(A, false, false, grid, s);

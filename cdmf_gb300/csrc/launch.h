@@ -55,7 +55,7 @@ void allow_smem(K kernel, size_t bytes) {
 
 // --- family 0 (launch.cu, CDMF_LAUNCH_PART 0): the length-binned sweeps ---
 
-// sweep_kernel over the bins; mode M_PLAIN, M_CSC, M_CSCP, M_CSR or M_CSR16.
+// sweep_kernel over the bins; mode M_PLAIN, M_CSC, M_CSCP, M_CSCQ, M_CSR or M_CSR16.
 template <int RT>
 void launch_rt(const SweepArgs& A, int mode, bool sub, bool add, unsigned grid, cudaStream_t s);
 

@@ -136,8 +136,8 @@ __device__ __forceinline__ void refresh_body(
                         acc = fmaf(w.w, h.w, acc);
                     }
                 }
-                acc = __fadd_rn(acc, __shfl_xor_sync(FULL, acc, 1));
-                acc = __fadd_rn(acc, __shfl_xor_sync(FULL, acc, 2));
+#pragma unroll
+                for (int o = 1; o < kRefG; o <<= 1) acc = __fadd_rn(acc, __shfl_xor_sync(FULL, acc, o));
                 const float got = __shfl_sync(FULL, acc, my_src);
                 if (my_round == r) dot = got;
             }

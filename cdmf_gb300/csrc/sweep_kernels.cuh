@@ -59,10 +59,11 @@ constexpr int M_CSRS = 4;   // M_CSR with the cross table staged in shared memor
 constexpr int M_CSR16 = 5;  // M_CSR reading 16-bit column indices (at most 65,536 columns)
 constexpr int M_CSRS16 = 6; // M_CSRS reading 16-bit column indices
 constexpr int M_CSCP = 7;   // M_CSC, software-pipelined at 4 blocks per SM (large matrices)
-template <int MODE> constexpr bool kIdx16 = MODE == M_CSR16 || MODE == M_CSRS16;
+constexpr int M_CSCQ = 8;   // M_CSCP reading 16-bit row offsets (rows below 2^19)
+template <int MODE> constexpr bool kIdx16 = MODE == M_CSR16 || MODE == M_CSRS16 || MODE == M_CSCQ;
 template <int MODE> constexpr bool kCsrFirst = MODE == M_CSR || MODE == M_CSR16;
 template <int MODE> constexpr bool kCsrShared = MODE == M_CSRS || MODE == M_CSRS16;
-template <int MODE> constexpr bool kCscFirst = MODE == M_CSC || MODE == M_CSCP;
+template <int MODE> constexpr bool kCscFirst = MODE == M_CSC || MODE == M_CSCP || MODE == M_CSCQ;
 
 // Resident blocks per SM asked of the compiler (register cap) and the
 // software-pipeline depth of the vector layout, per sweep mode.  Measured on
@@ -77,8 +78,8 @@ template <int MODE> constexpr bool kCscFirst = MODE == M_CSC || MODE == M_CSCP;
 //              latency.
 // On the 64-problem batch (short lines) M_CSCP measured 5 % slower than
 // M_CSC, so the engine takes it from 16M nonzeros up.
-template <int MODE> constexpr int kSweepBlocks = MODE == M_CSCP ? 4 : 6;
-template <int MODE> constexpr int kPipe = MODE == M_CSCP ? 2 : 0;
+template <int MODE> constexpr int kSweepBlocks = MODE == M_CSCP || MODE == M_CSCQ ? 4 : 6;
+template <int MODE> constexpr int kPipe = MODE == M_CSCP || MODE == M_CSCQ ? 2 : 0;
 
 struct XTask {            // one chunk of a split line
     uint32_t line, beg, end, slot;
@@ -114,7 +115,8 @@ struct SweepArgs {
     uint32_t ncross;               // M_CSRS: entries of the cross table (columns)
     uint32_t group_short;          // group lines up to this length: interleaved layout
     uint32_t group_lanes;          // lanes per group-bin line: 4 or 8
-    const uint16_t* __restrict__ idx16;   // M_CSR16 / M_CSRS16: the column indices, 16 bits each
+    const uint16_t* __restrict__ idx16;   // M_CSR16 / M_CSRS16: the column indices; M_CSCQ: the row offsets
+    const uint32_t* __restrict__ cseg;    // M_CSCQ: per column, kCSeg segment ends (see RowDec)
 };
 
 // The cross table of an M_CSRS sweep, as three float planes (a | c | y) in
@@ -297,10 +299,40 @@ __device__ __forceinline__ void ld_idx4(const SweepArgs& A, uint32_t q, uint32_t
     }
 }
 
+// Index decoding.  M_CSCQ stores each row as its 16-bit offset inside a
+// segment of 65,536 rows; rows are sorted inside a column, so a column is cut
+// into at most kCSeg runs of one segment each, and cseg[kCSeg * j + h] holds
+// where run h of column j ends (the column's end from the last non-empty run
+// on).  A lane keeps the segment of its current position and moves forward as
+// its positions grow (they only grow inside one strided pass).  Other modes
+// read indices as stored.
+constexpr uint32_t kCSeg = 8;
+template <int MODE, bool ON = (MODE == M_CSCQ)>
+struct RowDec {
+    __device__ __forceinline__ void init(const SweepArgs&, uint32_t, uint32_t) {}
+    __device__ __forceinline__ uint32_t row(uint32_t, uint32_t raw) { return raw; }
+};
+template <int MODE>
+struct RowDec<MODE, true> {
+    const uint32_t* seg;
+    uint32_t hi, nxt;
+    __device__ __forceinline__ void init(const SweepArgs& A, uint32_t line, uint32_t q) {
+        seg = A.cseg + (size_t)line * kCSeg;
+        hi = 0;
+        nxt = __ldg(seg);
+        (void)row(q, 0);
+    }
+    __device__ __forceinline__ uint32_t row(uint32_t q, uint32_t raw) {
+        while (q >= nxt && hi < kCSeg - 1) nxt = __ldg(seg + ++hi);
+        return (hi << 16) | raw;
+    }
+};
+
 // One scalar element: update, store, accumulate.
 template <int RT, int MODE, bool SUB, bool ADD, class AccT>
-__device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, float dj, AccT& g, AccT& h) {
-    const uint32_t i = ld_idx1<MODE>(A, q);
+__device__ __forceinline__ void elem1(const SweepArgs& A, uint32_t q, float bj, float dj, AccT& g, AccT& h,
+                                      RowDec<MODE>& dec) {
+    const uint32_t i = dec.row(q, ld_idx1<MODE>(A, q));
     float r = Res<RT>::ld(A.res, q);
     float a, c, y;
     fetch<MODE>(A, i, a, c, y);
@@ -350,12 +382,12 @@ struct Chunk4 {
 // Update, store and accumulate the 4 elements of a loaded chunk at q.
 template <int RT, int MODE, bool SUB, bool ADD, class AccT>
 __device__ __forceinline__ void chunk4(const SweepArgs& A, uint32_t q, const Chunk4<RT, MODE>& C, float bj, float dj,
-                                       AccT& g, AccT& h) {
+                                       AccT& g, AccT& h, RowDec<MODE>& dec) {
     float r[4], y[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
         float a, c;
-        fetch<MODE>(A, C.idx(e), a, c, y[e]);
+        fetch<MODE>(A, dec.row(q + e, C.idx(e)), a, c, y[e]);
         r[e] = update<SUB, ADD>(C.res(e), a, c, bj, dj);
     }
     if (SUB || ADD) Res<RT>::st4(A.res, q, r);
@@ -371,12 +403,12 @@ __device__ __forceinline__ void chunk4(const SweepArgs& A, uint32_t q, const Chu
 // visit a lane's elements in increasing order, so their sums are identical.
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN, int PIPE>
 __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
-                                            float dj, float& gs, float& hs) {
+                                            float dj, float& gs, float& hs, RowDec<MODE>& dec) {
     Acc<KAHAN> g, h;
     uint32_t vbeg = (beg + 3u) & ~3u;
     if (vbeg > end) vbeg = end;
     const uint32_t vend = vbeg + ((end - vbeg) & ~3u);
-    if (lane < vbeg - beg) elem1<RT, MODE, SUB, ADD>(A, beg + lane, bj, dj, g, h);
+    if (lane < vbeg - beg) elem1<RT, MODE, SUB, ADD>(A, beg + lane, bj, dj, g, h, dec);
     uint32_t q = vbeg + 4u * lane;
     if constexpr (PIPE > 0) {
         constexpr uint32_t STEP = 4u * S;
@@ -393,7 +425,7 @@ __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, ui
                     if (qn + u * STEP < vend) nxt[u].load(A, qn + u * STEP);
 #pragma unroll
                 for (int u = 0; u < PIPE; ++u)
-                    if (q + u * STEP < vend) chunk4<RT, MODE, SUB, ADD>(A, q + u * STEP, cur[u], bj, dj, g, h);
+                    if (q + u * STEP < vend) chunk4<RT, MODE, SUB, ADD>(A, q + u * STEP, cur[u], bj, dj, g, h, dec);
                 if (qn >= vend) break;
                 q = qn;
 #pragma unroll
@@ -416,7 +448,7 @@ __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, ui
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 float a, c;
-                fetch<MODE>(A, iv[u][e], a, c, y[e]);
+                fetch<MODE>(A, dec.row(q + 4u * S * u + e, iv[u][e]), a, c, y[e]);
                 r[u][e] = update<SUB, ADD>(r[u][e], a, c, bj, dj);
             }
             if (SUB || ADD) Res<RT>::st4(A.res, q + 4u * S * u, r[u]);
@@ -432,14 +464,14 @@ __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, ui
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             float a, c;
-            fetch<MODE>(A, iv[e], a, c, y[e]);
+            fetch<MODE>(A, dec.row(q + e, iv[e]), a, c, y[e]);
             r[e] = update<SUB, ADD>(r[e], a, c, bj, dj);
         }
         if (SUB || ADD) Res<RT>::st4(A.res, q, r);
 #pragma unroll
         for (int e = 0; e < 4; ++e) accumulate(g, h, y[e], r[e]);
     }
-    if (lane < end - vend) elem1<RT, MODE, SUB, ADD>(A, vend + lane, bj, dj, g, h);
+    if (lane < end - vend) elem1<RT, MODE, SUB, ADD>(A, vend + lane, bj, dj, g, h, dec);
     gs = g.value();
     hs = h.value();
 }
@@ -449,7 +481,7 @@ __device__ __forceinline__ void strided_vec(const SweepArgs& A, uint32_t beg, ui
 // gather.  ILP nonzeros per lane are in flight per step.
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
 __device__ __forceinline__ void strided_il(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
-                                           float dj, float& gs, float& hs) {
+                                           float dj, float& gs, float& hs, RowDec<MODE>& dec) {
     Acc<KAHAN> g, h;
     uint32_t q = beg + lane;
     for (; q + (uint32_t)S * (kIlp - 1) < end; q += (uint32_t)S * kIlp) {
@@ -461,14 +493,14 @@ __device__ __forceinline__ void strided_il(const SweepArgs& A, uint32_t beg, uin
             r[u] = Res<RT>::ld(A.res, q + S * u);
         }
 #pragma unroll
-        for (int u = 0; u < kIlp; ++u) fetch<MODE>(A, iv[u], a[u], c[u], y[u]);
+        for (int u = 0; u < kIlp; ++u) fetch<MODE>(A, dec.row(q + S * u, iv[u]), a[u], c[u], y[u]);
 #pragma unroll
         for (int u = 0; u < kIlp; ++u) {
             if (SUB || ADD) r[u] = Res<RT>::st(A.res, q + S * u, update<SUB, ADD>(r[u], a[u], c[u], bj, dj));
             accumulate(g, h, y[u], r[u]);
         }
     }
-    for (; q < end; q += S) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
+    for (; q < end; q += S) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h, dec);
     gs = g.value();
     hs = h.value();
 }
@@ -484,12 +516,14 @@ constexpr int kThreadUnroll = 4;
 // flight; 8-nonzero chunks; staging the streams through shared memory with
 // cp.async, which takes L1 capacity from the gather tables.)
 template <int RT, int MODE, bool SUB, bool ADD, int S, bool KAHAN>
-__device__ __forceinline__ void strided(const SweepArgs& A, uint32_t beg, uint32_t end, uint32_t lane, float bj,
-                                        float dj, float& gs, float& hs) {
+__device__ __forceinline__ void strided(const SweepArgs& A, uint32_t line, uint32_t beg, uint32_t end, uint32_t lane,
+                                        float bj, float dj, float& gs, float& hs) {
+    RowDec<MODE> dec;
+    dec.init(A, line, beg);
     if (S <= 8 && end - beg <= A.group_short)
-        strided_il<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs);
+        strided_il<RT, MODE, SUB, ADD, S, KAHAN>(A, beg, end, lane, bj, dj, gs, hs, dec);
     else
-        strided_vec<RT, MODE, SUB, ADD, S, KAHAN, kPipe<MODE>>(A, beg, end, lane, bj, dj, gs, hs);
+        strided_vec<RT, MODE, SUB, ADD, S, KAHAN, kPipe<MODE>>(A, beg, end, lane, bj, dj, gs, hs, dec);
 }
 
 template <int WIDTH = 32>
@@ -558,7 +592,7 @@ __device__ __forceinline__ void group_line(const SweepArgs& A, uint32_t b, uint3
     float bj = 0.0f, dj = 0.0f;
     if (valid) line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
     float g = 0.0f, h = 0.0f;
-    strided<RT, MODE, SUB, ADD, L, false>(A, beg, end, sub, bj, dj, g, h);
+    strided<RT, MODE, SUB, ADD, L, false>(A, j, beg, end, sub, bj, dj, g, h);
     warp_sum2<L>(g, h);
     if (valid && sub == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
 }
@@ -572,7 +606,7 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
         float bj, dj;
         line_scalars<MODE, SUB, ADD>(A, T.line, bj, dj);
         float g = 0.0f, h = 0.0f;
-        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, T.beg, T.end, tid, bj, dj, g, h);
+        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, T.line, T.beg, T.end, tid, bj, dj, g, h);
         cta_sum2<Team>(g, h);
         int& last = *Team::flag();
         if (tid == 0) {
@@ -603,7 +637,7 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
         float bj, dj;
         line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
         float g = 0.0f, h = 0.0f;
-        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, beg, end, tid, bj, dj, g, h);
+        strided<RT, MODE, SUB, ADD, kBlock, RT != 0>(A, j, beg, end, tid, bj, dj, g, h);
         cta_sum2<Team>(g, h);
         if (tid == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
         return;
@@ -619,9 +653,9 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
         line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
         float g = 0.0f, h = 0.0f;
         if (RT != 0 && end - beg > kKahanMin)
-            strided<RT, MODE, SUB, ADD, 32, true>(A, beg, end, lane, bj, dj, g, h);
+            strided<RT, MODE, SUB, ADD, 32, true>(A, j, beg, end, lane, bj, dj, g, h);
         else
-            strided<RT, MODE, SUB, ADD, 32, false>(A, beg, end, lane, bj, dj, g, h);
+            strided<RT, MODE, SUB, ADD, 32, false>(A, j, beg, end, lane, bj, dj, g, h);
         warp_sum2(g, h);
         if (lane == 0) finish_line<MODE>(A, j, end - beg, g, h, bj, dj);
         return;
@@ -640,9 +674,11 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
     const uint32_t len = end - beg;
     float bj, dj;
     line_scalars<MODE, SUB, ADD>(A, j, bj, dj);
+    RowDec<MODE> dec;
+    dec.init(A, j, beg);
     if (MODE == M_DUAL) {
         Acc<false> g, h;
-        for (uint32_t q = beg; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
+        for (uint32_t q = beg; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h, dec);
         A.out[j] = g.s;
         A.out2[j] = h.s;
         return;
@@ -666,12 +702,12 @@ __device__ __forceinline__ void sweep_block(const SweepArgs& A, uint32_t b) {
 #pragma unroll
         for (int e = 0; e < kThreadUnroll; ++e) {
             float a, c, y;
-            fetch<MODE>(A, iv[e], a, c, y);
+            fetch<MODE>(A, dec.row(q + e, iv[e]), a, c, y);
             if (SUB || ADD) r[e] = Res<RT>::st(A.res, q + e, update<SUB, ADD>(r[e], a, c, bj, dj));
             accumulate(g, h, y, r[e]);
         }
     }
-    for (; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h);
+    for (; q < end; ++q) elem1<RT, MODE, SUB, ADD>(A, q, bj, dj, g, h, dec);
     write_line<MODE>(A, j, __fdiv_rn(g.s, h.s), bj, dj);
 }
 

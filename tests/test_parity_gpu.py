@@ -485,3 +485,36 @@ def test_sixteen_bit_column_indices_match(cpu_scale, residual, monkeypatch):
     assert np.array_equal(rm1, rm2)
     for key in ("W", "H", "res_csc", "res_csr"):
         assert np.array_equal(bits(s1[key]), bits(s2[key])), key
+
+
+@pytest.fixture(scope="module")
+def large_tall():
+    """17.5M nonzeros over 300,000 rows: above the 16M-nonzero threshold of the
+    pipelined CSC sweep, with rows in five segments of 65,536."""
+    return synth.generate(m=300_000, n=4_000, nnz_total=17_500_000, test_fraction=0.01, row_alpha=0.9,
+                          row_max=2_000, col_alpha=0.9, col_cap=60_000, rank=6, seed=5)
+
+
+@pytest.mark.parametrize("residual", ["f32", "bf16"])
+def test_sixteen_bit_row_offsets_match(large_tall, residual, monkeypatch):
+    """From 16M nonzeros, matrices with at most 8 * 65,536 rows stream the CSC
+    row indices of the first CSC sweep as 16-bit offsets inside 65,536-row
+    segments (each column's segment ends in a small table); the result must
+    equal the 32-bit path bit for bit (CDMF_NO_IDX16 turns both narrow copies
+    off at create)."""
+    R = large_tall
+    assert R.nnz >= 16 << 20 and 65536 < R.m <= 8 << 16
+    k = 8
+    W0 = synth.initial_w(k, R.m, seed=0)
+    out = []
+    for off in (False, True):
+        if off:
+            monkeypatch.setenv("CDMF_NO_IDX16", "1")
+        with engine.Engine(R, k, 0.05, 2, 1, residual=residual) as e:
+            e.set_factors(W0)
+            rm = e.run(2)
+            out.append((rm, e.state()))
+    (rm1, s1), (rm2, s2) = out
+    assert np.array_equal(rm1, rm2)
+    for key in ("W", "H", "res_csc", "res_csr"):
+        assert np.array_equal(bits(s1[key]), bits(s2[key])), key
