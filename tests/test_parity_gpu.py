@@ -497,11 +497,12 @@ def large_tall():
 
 @pytest.mark.parametrize("residual", ["f32", "bf16"])
 def test_sixteen_bit_row_offsets_match(large_tall, residual, monkeypatch):
-    """From 16M nonzeros, matrices with at most 8 * 65,536 rows stream the CSC
-    row indices of the first CSC sweep as 16-bit offsets inside 65,536-row
-    segments (each column's segment ends in a small table); the result must
-    equal the 32-bit path bit for bit (CDMF_NO_IDX16 turns both narrow copies
-    off at create)."""
+    """From 16M nonzeros, FP32 runs on matrices with at most 8 * 65,536 rows
+    stream the CSC row indices of the first CSC sweep as 16-bit offsets inside
+    65,536-row segments (each column's segment ends in a small table); the
+    result must equal the 32-bit path bit for bit (CDMF_NO_IDX16 turns both
+    narrow copies off at create).  BF16 runs keep 32-bit row indices: the
+    comparison then covers the 16-bit column indices alone."""
     R = large_tall
     assert R.nnz >= 16 << 20 and 65536 < R.m <= 8 << 16
     k = 8
