@@ -774,6 +774,22 @@ __global__ void __launch_bounds__(kBlock) flush_kernel(const uint32_t* __restric
 // order, (pred - v)^2 in double, NaN terms skipped but counted.  Fixed grid;
 // block partials in double; the last block adds them in block order and
 // writes sqrt(sum / nnz_test) and the NaN count.
+// float -> double, exactly, without the FP64 pipe for normal values: the
+// exponent is rebiased and the mantissa shifted with integer operations (the
+// GB300's FP64 units are few, and the test RMSE widens k products per test
+// entry).  Zero keeps its sign; subnormals, infinities and NaN take the
+// conversion instruction.  Same value as (double)x for every float.
+__device__ __forceinline__ double widen(float x) {
+    const uint32_t u = __float_as_uint(x);
+    const uint32_t e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) {
+        if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+        return (double)x;
+    }
+    const uint32_t hi = (u & 0x80000000u) | ((e + (1023u - 127u)) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)((u & 7u) << 29));
+}
+
 // Block `bid` of `nblk` blocks of one test-RMSE reduction.
 template <class VT>
 __device__ __forceinline__ void rmse_body(const uint32_t* __restrict__ row, const uint32_t* __restrict__ col,
@@ -787,7 +803,7 @@ __device__ __forceinline__ void rmse_body(const uint32_t* __restrict__ row, cons
         const uint32_t i = row[e], j = col[e];
         double pred = 0.0;
         for (uint32_t t = 0; t < k; ++t)
-            pred = __dadd_rn(pred, (double)__fmul_rn(__ldg(W + (size_t)t * m + i), __ldg(H + (size_t)t * n + j)));
+            pred = __dadd_rn(pred, widen(__fmul_rn(__ldg(W + (size_t)t * m + i), __ldg(H + (size_t)t * n + j))));
         const double dv = __dsub_rn(pred, (double)val[e]);
         const double tmp = __dmul_rn(dv, dv);
         if (!isnan(tmp)) acc = __dadd_rn(acc, tmp);
