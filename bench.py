@@ -13,6 +13,8 @@ Printed as one JSON line (rank 0):
             with a per-iteration RMSE read-back, download of W and H
   roofline -- the sweep kernel: compulsory bytes per launch / mean launch time
   cpu_baseline -- the oracle CPU port of the reference engine on the host cores
+  k32    -- the same matrix at rank 32, the workload's other rank (updates/s,
+            BF16 and the FP32 comparison)
   batch64 -- the 64 uneven problems in one batched run against the same
             problems run one after another (--no-batch leaves it out)
 
@@ -270,7 +272,7 @@ def main():
     k, lam, T = run["k"], run["lambda_"], run["maxinneriter"]
     W0 = synth.initial_w(k, R.m, seed=rank)
 
-    def measure(residual):
+    def measure(residual, k=k, W0=W0):
         """Device-resident timing of args.steps outer iterations + a roofline pass."""
         t_create = time.perf_counter()
         e = engine.Engine(R, k, lam, maxiter=max(args.steps, args.e2e_outer), maxinneriter=T, residual=residual,
@@ -304,6 +306,13 @@ def main():
 
     head = measure(args.residual)
     comp = measure(args.compare) if args.compare != "none" else None
+    # the same matrix at the workload's other rank, k = 32 (both residuals)
+    k32 = None
+    if not args.quick and args.k == 64:
+        W32 = synth.initial_w(32, R.m, seed=rank)
+        k32 = {"residual": measure(args.residual, 32, W32)}
+        if args.compare != "none":
+            k32["compare"] = measure(args.compare, 32, W32)
     value, t_ms, launches = head["value"], head["t_ms"], head["launches"]
     achieved, bytes_launch, mean_launch_s = head["achieved"], head["bytes_launch"], head["mean_launch_s"]
     test_rmse = head["test_rmse"]
@@ -369,6 +378,17 @@ def main():
     if fmt is not None:
         line["formats"] = fmt
     line["rmse_ms_per_outer"] = head["rmse_ms_per_outer"]
+    if k32 is not None:
+        a = k32["residual"]
+        line["k32"] = {"value": a["value"], "unit": UNIT, "residual": args.residual,
+                       "ms_per_step": a["t_ms"] / args.steps, "test_rmse": a["test_rmse"],
+                       "roofline_frac": a["achieved"] / peak, "hbm_gbs_sweeps": a["achieved"]}
+        if "compare" in k32:
+            c = k32["compare"]
+            line["k32"]["comparison"] = {"residual": args.compare, "value": c["value"],
+                                         "ms_per_step": c["t_ms"] / args.steps, "test_rmse": c["test_rmse"],
+                                         "roofline_frac": c["achieved"] / peak}
+            line["k32"]["mixed_vs_fp32"] = a["value"] / c["value"] if args.compare == "f32" else None
     if batch is not None:
         line["batch64"] = batch
     print(json.dumps(line), flush=True)
