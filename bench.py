@@ -522,15 +522,20 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
     kw = dict(residual=args.residual, device=device, version=args.version, use_graph=bool(args.graph),
               relabel=bool(args.relabel), layout=args.layout)
     engine.train(Rp, Wp, k, lam, 1, T, H=Hp, inplace=True, **kw)  # warm the context
-    Wp[...] = W0
-    dist.barrier()
-    t0 = time.perf_counter()
-    _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, H=Hp, inplace=True, **kw)
-    e2e_s = dist.max(time.perf_counter() - t0)
+    # three timed calls, each from the same W0; the median call is reported
+    times = []
+    for _ in range(3):
+        Wp[...] = W0
+        dist.barrier()
+        t0 = time.perf_counter()
+        _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, H=Hp, inplace=True, **kw)
+        times.append(dist.max(time.perf_counter() - t0))
+    e2e_s = statistics.median(times)
     e2e_value = ws * k * args.e2e_outer / e2e_s
     return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "step": f"one cdmf_cuda_train call: upload, {args.e2e_outer} outer iterations, download",
-            "seconds": e2e_s, "test_rmse": float(e2e_rm[-1])}
+            "step": f"one cdmf_cuda_train call: upload, {args.e2e_outer} outer iterations, download "
+                    f"(median of {len(times)} calls)",
+            "seconds": e2e_s, "seconds_all": times, "test_rmse": float(e2e_rm[-1])}
 
 
 if __name__ == "__main__":
