@@ -959,6 +959,10 @@ int do_outer_graph(cdmf_handle* h, int oiter, double* rmse_dst) {
 }
 
 int replan(cdmf_handle* h, const BinCfg& cfg) {
+    // the captured outer iterations hold the old bins' arrays and counts
+    CU(h, cudaStreamSynchronize(h->s));
+    for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
+    h->graphs.clear();
     free_bins(h, h->csr);
     free_bins(h, h->csc);
     h->cfg = cfg;
@@ -998,8 +1002,14 @@ struct TuneKey {
         return std::tie(m, n, nnz, rt, relabeled) < std::tie(o.m, o.n, o.nnz, o.rt, o.relabeled);
     }
 };
-std::map<TuneKey, BinCfg>& tune_cache() {
-    static std::map<TuneKey, BinCfg> c;
+// the autotuner's pick for a shape: the bin limits and the lanes per
+// group-bin line
+struct TunePick {
+    BinCfg cfg;
+    uint32_t lanes;
+};
+std::map<TuneKey, TunePick>& tune_cache() {
+    static std::map<TuneKey, TunePick> c;
     return c;
 }
 std::mutex& tune_mutex() {
@@ -1680,45 +1690,67 @@ int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms) {
     const TuneKey key{h->m, h->n, h->nnz, h->rt, h->relabeled ? 1 : 0};
     int r;
     BinCfg best = h->cfg;
+    uint32_t best_lanes = h->group_lanes;
     double best_t = 0;
     bool cached = false;
     {
         std::lock_guard<std::mutex> lk(tune_mutex());
         auto it = tune_cache().find(key);
-        if (it != tune_cache().end()) { best = it->second; cached = true; }
+        if (it != tune_cache().end()) {
+            best = it->second.cfg;
+            best_lanes = it->second.lanes;
+            cached = true;
+        }
     }
     if (!cached) {
         const bool prof = h->profiling;
         h->profiling = false;
-        // coordinate search over group_max, warp_max, cta_max, from the
-        // defaults (0 = no lane-group bin).  On the 480,189 x 17,770
-        // workload (BF16, k = 64) it moves the lines of 257-512 nonzeros from
-        // warps to lane groups: 29.36 -> 28.98 ms per outer iteration.
+        // coordinate search over group_max, warp_max, cta_max, the split
+        // chunk and the lanes per group-bin line, from the defaults (0 = no
+        // lane-group bin).  On the 480,189 x 17,770
+        // workload (BF16, k = 64) it moves the lines of 257-1,024 nonzeros
+        // from warps to lane groups: 29.34 -> 28.72 ms per outer iteration.
         if ((r = time_feature(h, 3, &best_t))) return r;
-        const uint32_t gvals[] = {0, 64, 128, 256, 512, 1024};
+        // (group lines sum without compensation, so the group limit stays at
+        // or below kKahanMin)
+        const uint32_t gvals[] = {0, 64, 128, 256, 512, 1024, 2048, 4096};
         const uint32_t wvals[] = {1024, 2048, 4096, 16384};
         const uint32_t cvals[] = {8192, 16384, 65536};
-        for (int dim = 0; dim < 3; ++dim) {
-            const uint32_t* vals = dim == 0 ? gvals : dim == 1 ? wvals : cvals;
-            const int nv = dim == 0 ? 6 : dim == 1 ? 4 : 3;
+        const uint32_t kvals[] = {8192, 16384, 32768};
+        static_assert(4096 <= kKahanMin, "group lines must not need compensated sums");
+        for (int dim = 0; dim < 4; ++dim) {
+            const uint32_t* vals = dim == 0 ? gvals : dim == 1 ? wvals : dim == 2 ? cvals : kvals;
+            const int nv = dim == 0 ? 8 : dim == 1 ? 4 : 3;
             BinCfg base = best;
             for (int v = 0; v < nv; ++v) {
                 BinCfg c = base;
                 if (dim == 0) c.group_max = vals[v] ? vals[v] : c.thread_max;
                 if (dim == 1) c.warp_max = vals[v];
                 if (dim == 2) c.cta_max = vals[v];
-                if (c.group_max > c.warp_max || c.warp_max > c.cta_max) continue;
-                if (c.group_max == best.group_max && c.warp_max == best.warp_max && c.cta_max == best.cta_max) continue;
+                if (dim == 3) c.chunk = vals[v];
+                if (c.group_max > c.warp_max || c.warp_max > c.cta_max || c.chunk > c.cta_max) continue;
+                if (c.group_max == best.group_max && c.warp_max == best.warp_max && c.cta_max == best.cta_max &&
+                    c.chunk == best.chunk)
+                    continue;
                 if ((r = replan(h, c))) return r;
                 double t = 0;
                 if ((r = time_feature(h, 3, &t))) return r;
                 if (t < best_t) { best_t = t; best = c; }
             }
         }
+        {   // the other lane count for the group bin
+            const uint32_t lanes = best_lanes == 4 ? 8 : 4;
+            h->group_lanes = lanes;
+            if ((r = replan(h, best))) return r;
+            double t = 0;
+            if ((r = time_feature(h, 3, &t))) return r;
+            if (t < best_t) { best_t = t; best_lanes = lanes; }
+        }
         h->profiling = prof;
         std::lock_guard<std::mutex> lk(tune_mutex());
-        tune_cache()[key] = best;
+        tune_cache()[key] = TunePick{best, best_lanes};
     }
+    h->group_lanes = best_lanes;
     if ((r = replan(h, best))) return r;
     // the timing sweeps used the factors and residual as scratch
     if ((r = cdmf_cuda_set_factors(h, nullptr, nullptr))) return r;

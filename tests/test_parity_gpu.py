@@ -334,7 +334,7 @@ def test_autotune_and_bincfg(cpu_scale):
         cfg, ms = e.autotune()
         assert ms > 0 and cfg["thread_max"] <= cfg["warp_max"] <= cfg["cta_max"]
         assert e.bincfg() == cfg
-        for plan in (cfg, dict(group_max=0, warp_max=1024, cta_max=8192)):
+        for plan in (cfg, dict(group_max=0, warp_max=1024, cta_max=8192, chunk=4096)):
             e.set_bincfg(**plan)
             e.set_factors(W0)
             rm = e.run(run["maxiter"])
@@ -346,6 +346,29 @@ def test_autotune_and_bincfg(cpu_scale):
     with pytest.raises(Exception):
         with engine.Engine(R, run["k"], run["lambda_"], 1, 1) as e:
             e.set_bincfg(warp_max=100, cta_max=50)
+
+
+def test_bincfg_change_after_graph_runs(cpu_scale):
+    """A new bin plan after outer iterations were captured as CUDA graphs
+    drops those graphs: the next runs take the new plan, bit for bit as an
+    engine created with it."""
+    R, run, W0, ref = cpu_scale
+    plan = dict(group_max=0, warp_max=1024, cta_max=8192, chunk=4096)
+    args = (R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"])
+    with engine.Engine(*args, use_graph=True) as e:
+        e.set_factors(W0)
+        e.run(2)
+        e.set_bincfg(**plan)
+        e.set_factors(W0)
+        rm1 = e.run(2)
+        W1, H1 = e.factors()
+    with engine.Engine(*args, use_graph=True) as f:
+        f.set_bincfg(**plan)
+        f.set_factors(W0)
+        rm2 = f.run(2)
+        W2, H2 = f.factors()
+    assert np.array_equal(rm1, rm2)
+    assert np.array_equal(bits(W1), bits(W2)) and np.array_equal(bits(H1), bits(H2))
 
 
 # ---- cross-index-blocked layout ---------------------------------------------
