@@ -74,8 +74,8 @@ template <int MODE> constexpr bool kCscFirst = MODE == M_CSC || MODE == M_CSCP |
 //              205; 1 or 3 chunks at 4 blocks 213 / 201.
 //   CSR sweeps: 6 blocks, no pipeline 216; 5 blocks 220; 4 blocks, 2 chunks
 //              231; 6 blocks with a pipeline spill (40 registers): 411.  They
-//              are bound by L1 data-pipe wavefronts (81 % of peak), not by
-//              latency.
+//              are bound by L1 data-pipe wavefronts (82-86 % of peak), not
+//              by latency.
 // On the 64-problem batch (short lines) M_CSCP measured 5 % slower than
 // M_CSC, so the engine takes it from 16M nonzeros up.
 template <int MODE> constexpr int kSweepBlocks = MODE == M_CSCP || MODE == M_CSCQ ? 4 : 6;

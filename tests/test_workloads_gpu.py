@@ -11,7 +11,9 @@ after every outer iteration:
   - FP16 and BF16: on the trajectory of the CPU model of the 16-bit mode
     (oracle/mixed_model.c, the engine's refresh schedule) to within twice the
     reference's FP32 error + 2e-5;
-  - reference order (Jester-shaped): the FP32 oracle's RMSE to 1e-12.
+  - reference order (Jester-shaped): the FP32 oracle's RMSE to 1e-12;
+  - the benchmark's options (CUDA graphs, autotuned bins) on the Netflix
+    shapes: the same bounds.
 """
 import json
 import os
@@ -109,3 +111,23 @@ def test_reference_order_matches_fp32_oracle(workload):
         pytest.skip("one thread per line is slow on the 67k-nonzero columns; the Jester shape covers it")
     rm = _run(R, W0, g, residual="f32", reduce="sequential")
     assert np.max(np.abs(rm - np.asarray(g["rmse_f32"]))) <= SEQ_ATOL, (rm - np.asarray(g["rmse_f32"])).tolist()
+
+
+@pytest.mark.parametrize("residual", ["f32", "bf16"])
+def test_benchmark_options(workload, residual):
+    """The benchmark's own engine options -- outer iterations replayed as CUDA
+    graphs, bin limits picked by the autotuner -- on the Netflix-shaped
+    workloads it measures, held to the same trajectories."""
+    name, R, W0, g = workload
+    if not name.startswith("netflix_shape"):
+        pytest.skip("the benchmark runs the Netflix-shaped workload")
+    rm = _run(R, W0, g, residual=residual, use_graph=True, autotune=True)
+    r32, r64 = np.asarray(g["rmse_f32"]), np.asarray(g["rmse_f64"])
+    if residual == "f32":
+        bound = np.maximum(FP32_FLOOR, 2 * np.abs(r32 - r64))
+        assert np.all(np.abs(rm - r64) <= bound), (name, (rm - r64).tolist(), bound.tolist())
+        return
+    assert np.all(np.abs(rm - r64) <= MIXED_ATOL), (name, residual, (rm - r64).tolist())
+    model = np.asarray(g["model_" + residual])
+    tol = 2 * np.abs(r32 - r64) + MODEL_ATOL
+    assert np.all(np.abs(rm - model) <= tol), (name, residual, (rm - model).tolist(), tol.tolist())
