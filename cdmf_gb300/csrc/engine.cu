@@ -222,7 +222,8 @@ struct cdmf_handle {
     uint32_t* smemq_queue = nullptr;
     // host copies of the line pointers (engine numbering) and the bin plan
     std::vector<uint32_t> hptr_r, hptr_c;
-    BinCfg cfg;
+    BinCfg cfg;                      // bin limits of the CSR copy (and of the CSC copy unless tuned apart)
+    BinCfg cfg_c;                    // bin limits of the CSC copy
     bool seq = false;
     // 16-bit residual modes: CSR->CSC position map, row-major factor copies
     uint32_t* to_csc = nullptr;
@@ -958,7 +959,7 @@ int do_outer_graph(cdmf_handle* h, int oiter, double* rmse_dst) {
     return CDMF_OK;
 }
 
-int replan(cdmf_handle* h, const BinCfg& cfg) {
+int replan(cdmf_handle* h, const BinCfg& cfg, const BinCfg& cfg_c) {
     // the captured outer iterations hold the old bins' arrays and counts
     CU(h, cudaStreamSynchronize(h->s));
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
@@ -966,12 +967,15 @@ int replan(cdmf_handle* h, const BinCfg& cfg) {
     free_bins(h, h->csr);
     free_bins(h, h->csc);
     h->cfg = cfg;
+    h->cfg_c = cfg_c;
     int r;
     if ((r = upload_bins(h, h->csr, plan_bins(h->hptr_r.data(), h->m, h->seq, cfg))) ||
-        (r = upload_bins(h, h->csc, plan_bins(h->hptr_c.data(), h->n, h->seq, cfg))))
+        (r = upload_bins(h, h->csc, plan_bins(h->hptr_c.data(), h->n, h->seq, cfg_c))))
         return r;
     return CDMF_OK;
 }
+
+int replan(cdmf_handle* h, const BinCfg& cfg) { return replan(h, cfg, cfg); }
 
 // Time of one steady-state feature (CSC + CSR sweep with subtract and
 // add-back) under the current bins, in ms; the state is scratch.
@@ -1005,7 +1009,7 @@ struct TuneKey {
 // the autotuner's pick for a shape: the bin limits and the lanes per
 // group-bin line
 struct TunePick {
-    BinCfg cfg;
+    BinCfg cfg, cfg_c;
     uint32_t lanes;
 };
 std::map<TuneKey, TunePick>& tune_cache() {
@@ -1290,6 +1294,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     }
     h->seq = seq;
     h->cfg = default_bins(N);
+    h->cfg_c = h->cfg;
     h->group_lanes = N >= kLargeNnz && h->rt != 0 ? 4 : 8;
     if (relabel_on_gpu) {
         h->hptr_r = std::move(G.hptr_r);
@@ -1689,7 +1694,7 @@ int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms) {
     }
     const TuneKey key{h->m, h->n, h->nnz, h->rt, h->relabeled ? 1 : 0};
     int r;
-    BinCfg best = h->cfg;
+    BinCfg best = h->cfg, best_c = h->cfg_c;
     uint32_t best_lanes = h->group_lanes;
     double best_t = 0;
     bool cached = false;
@@ -1698,6 +1703,7 @@ int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms) {
         auto it = tune_cache().find(key);
         if (it != tune_cache().end()) {
             best = it->second.cfg;
+            best_c = it->second.cfg_c;
             best_lanes = it->second.lanes;
             cached = true;
         }
@@ -1705,11 +1711,12 @@ int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms) {
     if (!cached) {
         const bool prof = h->profiling;
         h->profiling = false;
-        // coordinate search over group_max, warp_max, cta_max, the split
-        // chunk and the lanes per group-bin line, from the defaults (0 = no
-        // lane-group bin).  On the 480,189 x 17,770
-        // workload (BF16, k = 64) it moves the lines of 257-1,024 nonzeros
-        // from warps to lane groups: 29.34 -> 28.72 ms per outer iteration.
+        // coordinate search over group_max, warp_max, cta_max and the split
+        // chunk, from the defaults (0 = no lane-group bin): first one plan
+        // for both copies, then the CSC copy's plan alone; last the lanes per
+        // group-bin line.  On the 480,189 x 17,770 workload (BF16, k = 64) it
+        // moves the lines of 257-1,024 nonzeros from warps to lane groups:
+        // 29.34 -> 28.72 ms per outer iteration.
         if ((r = time_feature(h, 3, &best_t))) return r;
         // (group lines sum without compensation, so the group limit stays at
         // or below kKahanMin)
@@ -1718,40 +1725,47 @@ int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms) {
         const uint32_t cvals[] = {8192, 16384, 65536};
         const uint32_t kvals[] = {8192, 16384, 32768};
         static_assert(4096 <= kKahanMin, "group lines must not need compensated sums");
-        for (int dim = 0; dim < 4; ++dim) {
-            const uint32_t* vals = dim == 0 ? gvals : dim == 1 ? wvals : dim == 2 ? cvals : kvals;
-            const int nv = dim == 0 ? 8 : dim == 1 ? 4 : 3;
-            BinCfg base = best;
-            for (int v = 0; v < nv; ++v) {
-                BinCfg c = base;
-                if (dim == 0) c.group_max = vals[v] ? vals[v] : c.thread_max;
-                if (dim == 1) c.warp_max = vals[v];
-                if (dim == 2) c.cta_max = vals[v];
-                if (dim == 3) c.chunk = vals[v];
-                if (c.group_max > c.warp_max || c.warp_max > c.cta_max || c.chunk > c.cta_max) continue;
-                if (c.group_max == best.group_max && c.warp_max == best.warp_max && c.cta_max == best.cta_max &&
-                    c.chunk == best.chunk)
-                    continue;
-                if ((r = replan(h, c))) return r;
-                double t = 0;
-                if ((r = time_feature(h, 3, &t))) return r;
-                if (t < best_t) { best_t = t; best = c; }
+        for (int pass = 0; pass < 2; ++pass) {   // 0: both copies, 1: the CSC copy alone
+            if (pass == 1) best_c = best;
+            for (int dim = 0; dim < 4; ++dim) {
+                const uint32_t* vals = dim == 0 ? gvals : dim == 1 ? wvals : dim == 2 ? cvals : kvals;
+                const int nv = dim == 0 ? 8 : dim == 1 ? 4 : 3;
+                const BinCfg base = pass == 0 ? best : best_c;
+                for (int v = 0; v < nv; ++v) {
+                    BinCfg c = base;
+                    if (dim == 0) c.group_max = vals[v] ? vals[v] : c.thread_max;
+                    if (dim == 1) c.warp_max = vals[v];
+                    if (dim == 2) c.cta_max = vals[v];
+                    if (dim == 3) c.chunk = vals[v];
+                    if (c.group_max > c.warp_max || c.warp_max > c.cta_max || c.chunk > c.cta_max) continue;
+                    const BinCfg& cur = pass == 0 ? best : best_c;
+                    if (c.group_max == cur.group_max && c.warp_max == cur.warp_max && c.cta_max == cur.cta_max &&
+                        c.chunk == cur.chunk)
+                        continue;
+                    if ((r = pass == 0 ? replan(h, c) : replan(h, best, c))) return r;
+                    double t = 0;
+                    if ((r = time_feature(h, 3, &t))) return r;
+                    if (t < best_t) {
+                        best_t = t;
+                        (pass == 0 ? best : best_c) = c;
+                    }
+                }
             }
         }
         {   // the other lane count for the group bin
             const uint32_t lanes = best_lanes == 4 ? 8 : 4;
             h->group_lanes = lanes;
-            if ((r = replan(h, best))) return r;
+            if ((r = replan(h, best, best_c))) return r;
             double t = 0;
             if ((r = time_feature(h, 3, &t))) return r;
             if (t < best_t) { best_t = t; best_lanes = lanes; }
         }
         h->profiling = prof;
         std::lock_guard<std::mutex> lk(tune_mutex());
-        tune_cache()[key] = TunePick{best, best_lanes};
+        tune_cache()[key] = TunePick{best, best_c, best_lanes};
     }
     h->group_lanes = best_lanes;
-    if ((r = replan(h, best))) return r;
+    if ((r = replan(h, best, best_c))) return r;
     // the timing sweeps used the factors and residual as scratch
     if ((r = cdmf_cuda_set_factors(h, nullptr, nullptr))) return r;
     CU(h, cudaMemsetAsync(h->P, 0, sizeof(float2) * std::max<int64_t>(1, h->m), h->s));
