@@ -207,10 +207,13 @@ int cdmf_cuda_set_state(cdmf_handle* h, const float* W, const float* H, const fl
                         const float* res_csr, int next_oiter);
 int cdmf_cuda_set_profiling(cdmf_handle* h, int on);
 int cdmf_cuda_stats(const cdmf_handle* h, cdmf_stats* s);
-/* Bin thresholds: read, set (re-plans the bins), or pick by timing one
- * steady-state feature per candidate on this matrix (coordinate search over
- * group_max, warp_max, cta_max).  Autotuning uses the factors and residual
- * as scratch and leaves a fresh state (as cdmf_cuda_set_factors(h, NULL, NULL)). */
+/* Bin thresholds: read (the CSR copy's), set (re-plans the bins of both
+ * copies), or pick by timing three steady-state features per candidate on
+ * this matrix (coordinate search over group_max, warp_max, cta_max and chunk,
+ * first one plan for both copies, then the CSC copy's alone, and over the
+ * lanes per group-bin line).  A new plan drops the outer iterations already
+ * captured as CUDA graphs.  Autotuning uses the factors and residual as
+ * scratch and leaves a fresh state (as cdmf_cuda_set_factors(h, NULL, NULL)). */
 int cdmf_cuda_get_bincfg(const cdmf_handle* h, cdmf_bincfg* c);
 int cdmf_cuda_set_bincfg(cdmf_handle* h, const cdmf_bincfg* c);
 int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms);
