@@ -14,9 +14,9 @@
 // exits.  It is shared by all calls: calls that overlap on the GPU (from
 // several streams or threads at once) race on it and must be serialised by
 // the caller.  Its device address is looked up once per device, on the first
-// call made with that device current, and kept; make that first call before
-// any stream capture begins.  A device reset moves the array, so a caller
-// that resets a device does not call this entry point on it again.
+// call made with that device current, and kept.  A device reset moves the
+// array, so a caller that resets a device does not call this entry point on
+// it again.
 #include <cdmf_cuda.h>
 
 #include "sweep_kernels.cuh"

@@ -165,9 +165,8 @@ int cdmf_cuda_rmse_coo(uint32_t k, int64_t m, int64_t n, const float* W, const f
  * partials and three counters), held by every device that loads the library
  * until exit and shared by all calls: calls that overlap on the GPU race on
  * it, so the caller serialises them.  The first call on a device looks up the
- * array's device address and keeps it; make that first call before any
- * stream capture begins, and do not call again on a device after resetting
- * it (cudaDeviceReset), which moves the array.  Test sets larger than
+ * array's device address and keeps it; do not call again on a device after
+ * resetting it (cudaDeviceReset), which moves the array.  Test sets larger than
  * CDMF_NOALLOC_MAX_TEST entries (the reference counts entries in an int) are
  * rejected with CDMF_ERR_TOO_LARGE.  stream: a cudaStream_t, or NULL for the
  * default stream; the call copies the result to host memory and waits for
