@@ -529,13 +529,15 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
     # the timed calls reuse the limits it picked
     engine.train(Rp, Wp, k, lam, 1, T, H=Hp, inplace=True, **kw)
     # three timed calls, each from the same W0; the median call is reported
-    times = []
+    times, clocks = [], []
     for _ in range(3):
         Wp[...] = W0
         dist.barrier()
-        t0 = time.perf_counter()
-        _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, H=Hp, inplace=True, **kw)
-        times.append(dist.max(time.perf_counter() - t0))
+        with ClockSampler(device) as clk:
+            t0 = time.perf_counter()
+            _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, H=Hp, inplace=True, **kw)
+            times.append(dist.max(time.perf_counter() - t0))
+        clocks.append(clk.summary())
     e2e_s = statistics.median(times)
     e2e_value = ws * k * args.e2e_outer / e2e_s
     return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -543,7 +545,7 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
                     f"(median of {len(times)} calls" + ("; bin limits from the autotuner's per-shape cache, "
                                                          "filled by an untimed first call)" if args.autotune
                                                          else ")"),
-            "seconds": e2e_s, "seconds_all": times, "test_rmse": float(e2e_rm[-1])}
+            "seconds": e2e_s, "seconds_all": times, "clocks_per_call": clocks, "test_rmse": float(e2e_rm[-1])}
 
 
 if __name__ == "__main__":
