@@ -1001,9 +1001,9 @@ int time_feature(cdmf_handle* h, int reps, double* ms) {
 
 struct TuneKey {
     int64_t m, n, nnz;
-    int rt, relabeled;
+    int rt, relabeled, device;
     bool operator<(const TuneKey& o) const {
-        return std::tie(m, n, nnz, rt, relabeled) < std::tie(o.m, o.n, o.nnz, o.rt, o.relabeled);
+        return std::tie(m, n, nnz, rt, relabeled, device) < std::tie(o.m, o.n, o.nnz, o.rt, o.relabeled, o.device);
     }
 };
 // the autotuner's pick for a shape: the bin limits and the lanes per
@@ -1687,12 +1687,14 @@ int cdmf_cuda_set_bincfg(cdmf_handle* h, const cdmf_bincfg* c) {
 int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms) {
     if (!h) return CDMF_ERR_INVALID;
     CU(h, cudaSetDevice(h->o.device));
-    if (h->seq || h->tiles || h->nnz == 0 || h->o.maxinneriter <= 0) {
+    // nothing to pick where the sweeps do not run on the length bins: one
+    // thread per line (reference order), the tile kernel, the blocked layout
+    if (h->seq || h->tiles || h->blocked || h->nnz == 0 || h->o.maxinneriter <= 0) {
         if (chosen) cdmf_cuda_get_bincfg(h, chosen);
         if (best_ms) *best_ms = 0;
         return CDMF_OK;
     }
-    const TuneKey key{h->m, h->n, h->nnz, h->rt, h->relabeled ? 1 : 0};
+    const TuneKey key{h->m, h->n, h->nnz, h->rt, h->relabeled ? 1 : 0, h->o.device};
     int r;
     BinCfg best = h->cfg, best_c = h->cfg_c;
     uint32_t best_lanes = h->group_lanes;

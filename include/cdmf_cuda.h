@@ -212,7 +212,10 @@ int cdmf_cuda_stats(const cdmf_handle* h, cdmf_stats* s);
  * first one plan for both copies, then the CSC copy's alone, and over the
  * lanes per group-bin line).  A new plan drops the outer iterations already
  * captured as CUDA graphs.  Autotuning uses the factors and residual as
- * scratch and leaves a fresh state (as cdmf_cuda_set_factors(h, NULL, NULL)). */
+ * scratch and leaves a fresh state (as cdmf_cuda_set_factors(h, NULL, NULL)).
+ * Picks are kept per process for each (shape, residual type, numbering,
+ * device).  Handles whose sweeps do not use the bins (reduce = sequential,
+ * version 3, the blocked layout) are left as they are, with *best_ms = 0. */
 int cdmf_cuda_get_bincfg(const cdmf_handle* h, cdmf_bincfg* c);
 int cdmf_cuda_set_bincfg(cdmf_handle* h, const cdmf_bincfg* c);
 int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms);

@@ -348,6 +348,18 @@ def test_autotune_and_bincfg(cpu_scale):
             e.set_bincfg(warp_max=100, cta_max=50)
 
 
+@pytest.mark.parametrize("opts", [dict(layout="blocked"), dict(version=3), dict(reduce="sequential")])
+def test_autotune_leaves_unbinned_sweeps_alone(cpu_scale, opts):
+    """Handles whose sweeps do not run on the length bins (blocked layout,
+    tile kernel, reference order) get no search: the plan stays as created
+    and no time is reported."""
+    R, run, W0, ref = cpu_scale
+    with engine.Engine(R, run["k"], run["lambda_"], 1, 1, **opts) as e:
+        before = e.bincfg()
+        cfg, ms = e.autotune()
+        assert ms == 0 and cfg == before == e.bincfg()
+
+
 def test_bincfg_change_after_graph_runs(cpu_scale):
     """A new bin plan after outer iterations were captured as CUDA graphs
     drops those graphs: the next runs take the new plan, bit for bit as an
