@@ -11,6 +11,8 @@ Printed as one JSON line (rank 0):
   e2e    -- updates/s through cdmf_cuda_train (the reference's engine call)
             from page-locked host buffers: upload of R, 20 outer iterations
             with a per-iteration RMSE read-back, download of W and H
+            (median of 3 calls; SM clocks and the engine's phase times of
+            each call beside it)
   roofline -- the sweep kernel: compulsory bytes per launch / mean launch time
   cpu_baseline -- the oracle CPU port of the reference engine on the host cores
   k32    -- the same matrix at rank 32, the workload's other rank (updates/s,
@@ -500,6 +502,27 @@ def measure_formats(R, peak):
             "spmv_frac": spmv_bytes / spmv_ms / 1e6 / peak}
 
 
+def with_phase_times(fn):
+    """Runs fn() with the engine's stderr (the phase times that verbose
+    options print) captured; returns (fn's result, {phase: ms})."""
+    import re
+    sys.stderr.flush()
+    saved = os.dup(2)
+    with tempfile.TemporaryFile() as tf:
+        os.dup2(tf.fileno(), 2)
+        try:
+            out = fn()
+        finally:
+            os.dup2(saved, 2)
+            os.close(saved)
+        tf.seek(0)
+        text = tf.read().decode(errors="replace")
+    phases = {}
+    for kind, what, ms in re.findall(r"\[cdmf\] (train|create): (.+?)\s+([0-9.]+) ms", text):
+        phases[(what.strip() if kind == "train" else "create/" + what.strip())] = float(ms)
+    return out, phases
+
+
 def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
     """updates/s through cdmf_cuda_train from page-locked host buffers."""
     from cdmf_gb300 import engine, _lib
@@ -529,15 +552,18 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
     # the timed calls reuse the limits it picked
     engine.train(Rp, Wp, k, lam, 1, T, H=Hp, inplace=True, **kw)
     # three timed calls, each from the same W0; the median call is reported
-    times, clocks = [], []
+    # (verbose: the engine prints its phase times, recorded per call)
+    times, clocks, phases = [], [], []
     for _ in range(3):
         Wp[...] = W0
         dist.barrier()
         with ClockSampler(device) as clk:
             t0 = time.perf_counter()
-            _, _, e2e_rm = engine.train(Rp, Wp, k, lam, args.e2e_outer, T, H=Hp, inplace=True, **kw)
+            (_, _, e2e_rm), ph = with_phase_times(
+                lambda: engine.train(Rp, Wp, k, lam, args.e2e_outer, T, H=Hp, inplace=True, verbose=1, **kw))
             times.append(dist.max(time.perf_counter() - t0))
         clocks.append(clk.summary())
+        phases.append(ph)
     e2e_s = statistics.median(times)
     e2e_value = ws * k * args.e2e_outer / e2e_s
     return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -545,7 +571,8 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
                     f"(median of {len(times)} calls" + ("; bin limits from the autotuner's per-shape cache, "
                                                          "filled by an untimed first call)" if args.autotune
                                                          else ")"),
-            "seconds": e2e_s, "seconds_all": times, "clocks_per_call": clocks, "test_rmse": float(e2e_rm[-1])}
+            "seconds": e2e_s, "seconds_all": times, "clocks_per_call": clocks, "phases_ms_per_call": phases,
+            "test_rmse": float(e2e_rm[-1])}
 
 
 if __name__ == "__main__":

@@ -1023,6 +1023,76 @@ std::mutex& tune_mutex() {
 
 }  // namespace
 
+namespace {
+
+// cdmf_cuda_train's outer iterations, queued one ahead of the host: outer
+// iteration it + 1 is on the stream before the host waits for the RMSE of
+// outer iteration it, so the GPU does not sit idle while the host reads a
+// result, calls the callback and queues the next iteration.  The launches and
+// their order are those of cdmf_cuda_run(h, 1, ...) called once per outer
+// iteration, so are the results.  A non-finite residual at a refresh ends the
+// run with CDMF_ERR_NUMERIC after the callback of the outer iteration before
+// it, as the per-iteration calls did.  cb's ms: time since the first outer
+// iteration started, on the engine stream.
+int run_queued(cdmf_handle* h, double* rmse_out, cdmf_outer_cb cb, void* user) {
+    const int n = h->o.maxiter;
+    if (n <= 0) return CDMF_OK;
+    CU(h, cudaSetDevice(h->o.device));
+    const bool want_rmse = h->o.rmse_each_outer && h->nt > 0;
+    struct Slot {              // read back after each outer iteration
+        double rmse;
+        unsigned long long bad;   // non-finite refresh results so far
+    };
+    struct Res {
+        Slot* slots = nullptr;
+        std::vector<cudaEvent_t> ev;
+        ~Res() {
+            for (cudaEvent_t e : ev) cudaEventDestroy(e);
+            if (slots) cudaFreeHost(slots);
+        }
+    } res;
+    CU(h, cudaMallocHost((void**)&res.slots, sizeof(Slot) * (size_t)n));
+    res.ev.reserve(n);
+    for (int it = 0; it < n; ++it) {
+        cudaEvent_t e = nullptr;
+        CU(h, cudaEventCreate(&e));
+        res.ev.push_back(e);
+    }
+    h->refreshed = false;
+    h->marks.clear();
+    h->pool_used = 0;
+    if (h->rt != 0) CU(h, cudaMemsetAsync(h->nonfinite, 0, 8, h->s));
+    CU(h, cudaEventRecord(h->ev_start, h->s));
+    auto finish = [&](int it) -> int {
+        CU(h, cudaEventSynchronize(res.ev[it]));
+        if (h->rt != 0 && res.slots[it].bad)
+            return fail(h, CDMF_ERR_NUMERIC, "non-finite residual values at the refresh");
+        float ms = 0;
+        CU(h, cudaEventElapsedTime(&ms, h->ev_start, res.ev[it]));
+        const double rm = want_rmse ? res.slots[it].rmse : -1.0;
+        if (rmse_out) rmse_out[it] = rm;
+        if (cb) cb(it + 1, rm, ms, user);
+        return CDMF_OK;
+    };
+    // rmse_out on the device has maxiter + 1 slots: one per outer iteration
+    for (int it = 0; it < n; ++it) {
+        const int oiter = h->next_oiter;
+        int r = (h->o.use_graph && !h->profiling) ? do_outer_graph(h, oiter, h->rmse_out + it)
+                                                  : do_outer(h, oiter, h->rmse_out + it);
+        if (r) return r;
+        h->st.updates += h->o.k;
+        h->next_oiter++;
+        if (want_rmse)
+            CU(h, cudaMemcpyAsync(&res.slots[it].rmse, h->rmse_out + it, 8, cudaMemcpyDeviceToHost, h->s));
+        if (h->rt != 0) CU(h, cudaMemcpyAsync(&res.slots[it].bad, h->nonfinite, 8, cudaMemcpyDeviceToHost, h->s));
+        CU(h, cudaEventRecord(res.ev[it], h->s));
+        if (it > 0 && (r = finish(it - 1))) return r;
+    }
+    return finish(n - 1);
+}
+
+}  // namespace
+
 extern "C" {
 
 void cdmf_opts_default(cdmf_opts* o) {
@@ -1844,16 +1914,7 @@ int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* 
     phase("create");
     if ((r = cdmf_cuda_set_factors(h, W, nullptr))) { cdmf_cuda_destroy(h); return r; }
     phase("set_factors");
-    const bool want_rmse = o->rmse_each_outer && p->nnz_test > 0;
-    double total_ms = 0;
-    for (int it = 0; it < o->maxiter; ++it) {
-        double rm = 0;
-        if ((r = cdmf_cuda_run(h, 1, want_rmse ? &rm : nullptr))) { cdmf_cuda_destroy(h); return r; }
-        total_ms += h->st.train_ms;
-        if (rmse_out) rmse_out[it] = want_rmse ? rm : -1.0;
-        if (cb) cb(it + 1, want_rmse ? rm : -1.0, total_ms, user);
-    }
-    h->st.train_ms = total_ms;
+    if ((r = run_queued(h, rmse_out, cb, user))) { cdmf_cuda_destroy(h); return r; }
     phase("outer loop");
     r = cdmf_cuda_get_factors(h, W, H);
     phase("get_factors");

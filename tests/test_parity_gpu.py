@@ -18,6 +18,7 @@ Two reduction modes:
                 fro(x - r) = ||x - r||_F / ||r||_F; rel(x, r) = max |x - r| /
                 max(|r|, 0.1 * rms of r's feature vector).
 """
+import ctypes
 import json
 import os
 
@@ -25,7 +26,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, load_golden
-from cdmf_gb300 import engine, synth
+from cdmf_gb300 import _lib, engine, synth
 from oracle import oracle
 
 pytestmark = pytest.mark.gpu
@@ -274,6 +275,36 @@ def test_mixed_refresh_restores_exact_residual(cpu_scale):
     # further BF16 updates: it stays within a few BF16 ulps of the exact one
     err = np.abs(got - exact)
     assert np.sqrt(np.mean(err ** 2)) < 2e-2 and np.max(err) < 0.25
+
+
+@pytest.mark.parametrize("residual,graph", [("f32", False), ("bf16", True)])
+def test_train_queued_matches_run(cpu_scale, residual, graph):
+    """cdmf_cuda_train queues each outer iteration before it reads the
+    previous one's RMSE: factors and RMSE are those of an engine run one
+    outer iteration at a time, bit for bit, and the callback sees every
+    iteration in order, with its RMSE and growing times."""
+    R, run, W0, ref = cpu_scale
+    n, k = run["maxiter"], run["k"]
+    with engine.Engine(R, k, run["lambda_"], n, run["maxinneriter"], residual=residual, use_graph=graph) as e:
+        e.set_factors(W0)
+        rm1 = np.concatenate([e.run(1) for _ in range(n)])
+        W1, H1 = e.factors()
+    o = engine.make_opts(k, run["lambda_"], n, run["maxinneriter"], residual=residual, use_graph=graph)
+    p = engine._problem(R)
+    W2 = np.ascontiguousarray(W0, np.float32).copy()
+    H2 = np.zeros((k, R.n), np.float32)
+    rm2 = np.zeros(n)
+    seen = []
+    cb = _lib.OUTER_CB(lambda it, rmse, ms, user: seen.append((it, rmse, ms)))
+    st = _lib.load().cdmf_cuda_train(ctypes.byref(p), ctypes.byref(o), _lib.ptr(W2, ctypes.c_float),
+                                     _lib.ptr(H2, ctypes.c_float), _lib.ptr(rm2, ctypes.c_double), cb, None)
+    assert st == 0
+    assert np.array_equal(bits(W1), bits(W2)) and np.array_equal(bits(H1), bits(H2))
+    assert np.array_equal(rm1, rm2)
+    assert [s[0] for s in seen] == list(range(1, n + 1))
+    assert np.array_equal(np.array([s[1] for s in seen]), rm2)
+    ms = [s[2] for s in seen]
+    assert ms[0] > 0 and all(a <= b for a, b in zip(ms, ms[1:]))
 
 
 @pytest.mark.parametrize("version", [1, 3])
