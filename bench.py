@@ -11,8 +11,8 @@ Printed as one JSON line (rank 0):
   e2e    -- updates/s through cdmf_cuda_train (the reference's engine call)
             from page-locked host buffers: upload of R, 20 outer iterations
             with a per-iteration RMSE read-back, download of W and H
-            (median of 3 calls; SM clocks and the engine's phase times of
-            each call beside it)
+            (median of 3 calls; the SM clocks over the calls and the
+            engine's phase times of each call beside it)
   roofline -- the sweep kernel: compulsory bytes per launch / mean launch time
   cpu_baseline -- the oracle CPU port of the reference engine on the host cores
   k32    -- the same matrix at rank 32, the workload's other rank (updates/s,
@@ -105,6 +105,9 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
+            # nvidia-smi's start-up (NVML initialisation) makes driver calls of
+            # its own; let it finish before the timed work starts
+            time.sleep(1.0)
         except Exception:
             self.proc = None
             if self.f:
@@ -552,18 +555,19 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
     # the timed calls reuse the limits it picked
     engine.train(Rp, Wp, k, lam, 1, T, H=Hp, inplace=True, **kw)
     # three timed calls, each from the same W0; the median call is reported
-    # (verbose: the engine prints its phase times, recorded per call)
-    times, clocks, phases = [], [], []
-    for _ in range(3):
-        Wp[...] = W0
-        dist.barrier()
-        with ClockSampler(device) as clk:
+    # (verbose: the engine prints its phase times, recorded per call; one
+    # clock sampler runs through the three calls)
+    times, phases = [], []
+    with ClockSampler(device) as clk:
+        for _ in range(3):
+            Wp[...] = W0
+            dist.barrier()
             t0 = time.perf_counter()
             (_, _, e2e_rm), ph = with_phase_times(
                 lambda: engine.train(Rp, Wp, k, lam, args.e2e_outer, T, H=Hp, inplace=True, verbose=1, **kw))
             times.append(dist.max(time.perf_counter() - t0))
-        clocks.append(clk.summary())
-        phases.append(ph)
+            phases.append(ph)
+    clocks = clk.summary()
     e2e_s = statistics.median(times)
     e2e_value = ws * k * args.e2e_outer / e2e_s
     return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -571,7 +575,7 @@ def run_e2e(R, W0, k, lam, T, args, dist, ws, device):
                     f"(median of {len(times)} calls" + ("; bin limits from the autotuner's per-shape cache, "
                                                          "filled by an untimed first call)" if args.autotune
                                                          else ")"),
-            "seconds": e2e_s, "seconds_all": times, "clocks_per_call": clocks, "phases_ms_per_call": phases,
+            "seconds": e2e_s, "seconds_all": times, "clocks": clocks, "phases_ms_per_call": phases,
             "test_rmse": float(e2e_rm[-1])}
 
 
