@@ -1044,13 +1044,16 @@ int run_queued(cdmf_handle* h, double* rmse_out, cdmf_outer_cb cb, void* user) {
         unsigned long long bad;   // non-finite refresh results so far
     };
     struct Res {
+        cudaStream_t s;
         Slot* slots = nullptr;
         std::vector<cudaEvent_t> ev;
         ~Res() {
+            // (an early return can leave copies into slots on the stream)
+            cudaStreamSynchronize(s);
             for (cudaEvent_t e : ev) cudaEventDestroy(e);
             if (slots) cudaFreeHost(slots);
         }
-    } res;
+    } res{h->s};
     CU(h, cudaMallocHost((void**)&res.slots, sizeof(Slot) * (size_t)n));
     res.ev.reserve(n);
     for (int it = 0; it < n; ++it) {

@@ -307,6 +307,32 @@ def test_train_queued_matches_run(cpu_scale, residual, graph):
     assert ms[0] > 0 and all(a <= b for a, b in zip(ms, ms[1:]))
 
 
+@pytest.mark.parametrize("graph", [False, True])
+def test_train_stops_on_non_finite_refresh(cpu_scale, graph):
+    """A rating beyond FP16's range (65,504) leaves a non-finite FP16
+    residual: the refresh at the start of outer iteration 2 counts it, and
+    cdmf_cuda_train stops with CDMF_ERR_NUMERIC after the callback of outer
+    iteration 1, leaving the caller's factors untouched."""
+    from cdmf_gb300 import formats
+    R, run, W0, ref = cpu_scale
+    rows, cols, vals = R.coo()
+    vals = vals.copy()
+    vals[0] = 1e6
+    Rb = formats.from_coo(R.m, R.n, rows, cols, vals, R.te_row, R.te_col, R.te_val)
+    k = run["k"]
+    o = engine.make_opts(k, run["lambda_"], 4, 1, residual="f16", use_graph=graph)
+    p = engine._problem(Rb)
+    W = np.ascontiguousarray(W0, np.float32).copy()
+    H = np.zeros((k, Rb.n), np.float32)
+    seen = []
+    cb = _lib.OUTER_CB(lambda it, rmse, ms, user: seen.append(it))
+    st = _lib.load().cdmf_cuda_train(ctypes.byref(p), ctypes.byref(o), _lib.ptr(W, ctypes.c_float),
+                                     _lib.ptr(H, ctypes.c_float), None, cb, None)
+    assert st == -6, st   # CDMF_ERR_NUMERIC
+    assert seen == [1]
+    assert np.array_equal(bits(W), bits(np.ascontiguousarray(W0, np.float32)))
+
+
 @pytest.mark.parametrize("version", [1, 3])
 @pytest.mark.parametrize("residual", ["f32", "bf16"])
 def test_graph_replay_identical(cpu_scale, residual, version):
