@@ -289,16 +289,18 @@ int dalloc(cdmf_handle* h, T** p, size_t count) {
     return CDMF_OK;
 }
 
+// (branch-free reductions, so the compiler vectorises the scans)
 int check_compressed(const uint32_t* ptr, const uint32_t* idx, int64_t lines, int64_t cross, int64_t nnz) {
     if (!ptr || (nnz > 0 && !idx)) return CDMF_ERR_INVALID;
     if (ptr[0] != 0 || (int64_t)ptr[lines] != nnz) return CDMF_ERR_INVALID;
-    bool ok = true;
-#pragma omp parallel for schedule(static) reduction(&& : ok)
-    for (int64_t j = 0; j < lines; ++j) ok = ok && ptr[j] <= ptr[j + 1];
-    if (!ok) return CDMF_ERR_INVALID;
-#pragma omp parallel for schedule(static) reduction(&& : ok)
-    for (int64_t q = 0; q < nnz; ++q) ok = ok && (int64_t)idx[q] < cross;
-    return ok ? CDMF_OK : CDMF_ERR_INVALID;
+    int64_t down = 0;   // decreasing pointer pairs
+#pragma omp parallel for schedule(static) reduction(+ : down)
+    for (int64_t j = 0; j < lines; ++j) down += ptr[j] > ptr[j + 1];
+    if (down) return CDMF_ERR_INVALID;
+    uint32_t hi = 0;
+#pragma omp parallel for schedule(static) reduction(max : hi)
+    for (int64_t q = 0; q < nnz; ++q) hi = std::max(hi, idx[q]);
+    return nnz > 0 && (int64_t)hi >= cross ? CDMF_ERR_INVALID : CDMF_OK;
 }
 
 int upload_bins(cdmf_handle* h, DevBins& D, Bins&& B) {
@@ -1180,8 +1182,13 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     if (p->nnz > 0 && (!p->csr_val || !p->csc_val)) return CDMF_ERR_INVALID;
     if (p->nnz_test > 0) {
         if (!p->test_row || !p->test_col || !p->test_val) return CDMF_ERR_INVALID;
-        for (int64_t e = 0; e < p->nnz_test; ++e)
-            if ((int64_t)p->test_row[e] >= p->m || (int64_t)p->test_col[e] >= p->n) return CDMF_ERR_INVALID;
+        uint32_t hr = 0, hc = 0;
+#pragma omp parallel for schedule(static) reduction(max : hr, hc)
+        for (int64_t e = 0; e < p->nnz_test; ++e) {
+            hr = std::max(hr, p->test_row[e]);
+            hc = std::max(hc, p->test_col[e]);
+        }
+        if ((int64_t)hr >= p->m || (int64_t)hc >= p->n) return CDMF_ERR_INVALID;
     }
     phase("checks");
     int ndev = 0;

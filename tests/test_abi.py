@@ -70,6 +70,14 @@ def test_create_rejects_bad_structures():
     bad.te_row = R.te_row.copy()
     bad.te_row[0] = 6                                     # test row out of range
     assert _create(bad) == -1
+    bad = load_golden("simple")[0]
+    bad.te_col = R.te_col.copy()
+    bad.te_col[-1] = R.n                                  # test column out of range
+    assert _create(bad) == -1
+    bad = load_golden("simple")[0]
+    bad.csr_idx = R.csr_idx.copy()
+    bad.csr_idx[-1] = R.n                                 # last column index one past the end
+    assert _create(bad) == -1
     assert _create(R, k=0) == -1
     assert _create(R, lambda_=-1.0) == -1
     assert _create(R, residual=5) == -1
