@@ -345,9 +345,24 @@ int gpu_relabel(const cdmf_problem& p, cudaStream_t s, GpuRelabel& out, std::vec
         !S.get(&key_b, N))
         return CDMF_ERR_ALLOC;
 #define RC(x) do { if ((x) != cudaSuccess) return CDMF_ERR_CUDA; } while (0)
+    // the ratings are first read by csr_fill, after the sorts: they are
+    // uploaded on a side stream while the sorts run (queued below, after the
+    // sorts, so that a synchronous copy from pageable memory overlaps them too)
+    struct Side {
+        cudaStream_t s = nullptr;
+        cudaEvent_t done = nullptr;
+        ~Side() {
+            if (s) {
+                cudaStreamSynchronize(s);
+                cudaStreamDestroy(s);
+            }
+            if (done) cudaEventDestroy(done);
+        }
+    } side;
+    RC(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
+    RC(cudaEventCreateWithFlags(&side.done, cudaEventDisableTiming));
     RC(cudaMemcpyAsync(uptr, p.csr_row_ptr, 4 * (size_t)(m + 1), cudaMemcpyHostToDevice, s));
     RC(cudaMemcpyAsync(uidx, p.csr_col_idx, 4 * (size_t)N, cudaMemcpyHostToDevice, s));
-    RC(cudaMemcpyAsync(uval, p.csr_val, 4 * (size_t)N, cudaMemcpyHostToDevice, s));
     RC(cudaMemsetAsync(ccnt, 0, 4 * (size_t)n, s));
     // degree orders
     row_degrees<<<grid_for(m), kThreads, 0, s>>>(uptr, m, rkey, rid);
@@ -382,6 +397,9 @@ int gpu_relabel(const cdmf_problem& p, cudaStream_t s, GpuRelabel& out, std::vec
     RC(cudaGetLastError());
     tbv = tb;
     RC(cub::DeviceRadixSort::SortPairs(tmp, tbv, key_a, key_b, pos_a, out.csr_pos, N, 0, kbits, s));
+    RC(cudaMemcpyAsync(uval, p.csr_val, 4 * (size_t)N, cudaMemcpyHostToDevice, side.s));
+    RC(cudaEventRecord(side.done, side.s));
+    RC(cudaStreamWaitEvent(s, side.done, 0));
     csr_fill<<<grid_for(N), kThreads, 0, s>>>(key_b, out.csr_pos, uval, N, (uint64_t)n, out.csr_idx, out.csr_val, iota);
     RC(cudaGetLastError());
     // CSC: stable transposition
