@@ -1022,6 +1022,20 @@ std::mutex& tune_mutex() {
     static std::mutex mu;
     return mu;
 }
+TuneKey tune_key(const cdmf_handle* h) {
+    return TuneKey{h->m, h->n, h->nnz, h->rt, h->relabeled ? 1 : 0, h->o.device};
+}
+bool cached_pick(const TuneKey& key, TunePick* out) {
+    std::lock_guard<std::mutex> lk(tune_mutex());
+    auto it = tune_cache().find(key);
+    if (it == tune_cache().end()) return false;
+    *out = it->second;
+    return true;
+}
+bool same_cfg(const BinCfg& a, const BinCfg& b) {
+    return a.thread_max == b.thread_max && a.group_max == b.group_max && a.warp_max == b.warp_max &&
+           a.cta_max == b.cta_max && a.chunk == b.chunk;
+}
 
 }  // namespace
 
@@ -1376,6 +1390,14 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
     h->cfg = default_bins(N);
     h->cfg_c = h->cfg;
     h->group_lanes = N >= kLargeNnz && h->rt != 0 ? 4 : 8;
+    if (o->autotune && !seq && !h->tiles && !h->blocked) {   // a pick already made for this shape: plan with it
+        TunePick pick;
+        if (cached_pick(tune_key(h), &pick)) {
+            h->cfg = pick.cfg;
+            h->cfg_c = pick.cfg_c;
+            h->group_lanes = pick.lanes;
+        }
+    }
     if (relabel_on_gpu) {
         h->hptr_r = std::move(G.hptr_r);
         h->hptr_c = std::move(G.hptr_c);
@@ -1384,7 +1406,7 @@ int cdmf_cuda_create(const cdmf_problem* p, const cdmf_opts* o, cdmf_handle** ou
         h->hptr_c.assign(p->csc_col_ptr, p->csc_col_ptr + n + 1);
     }
     if ((r = upload_bins(h, h->csr, plan_bins(h->hptr_r.data(), m, seq, h->cfg))) ||
-        (r = upload_bins(h, h->csc, plan_bins(h->hptr_c.data(), n, seq, h->cfg))))
+        (r = upload_bins(h, h->csc, plan_bins(h->hptr_c.data(), n, seq, h->cfg_c))))
         return bail(r);
     if (h->rt != 0 && N > 0) {
         // the refresh's chunk start rows: the row holding nonzero c * kRefreshChunk, then the last row
@@ -1774,23 +1796,18 @@ int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms) {
         if (best_ms) *best_ms = 0;
         return CDMF_OK;
     }
-    const TuneKey key{h->m, h->n, h->nnz, h->rt, h->relabeled ? 1 : 0, h->o.device};
+    const TuneKey key = tune_key(h);
     int r;
     BinCfg best = h->cfg, best_c = h->cfg_c;
     uint32_t best_lanes = h->group_lanes;
     double best_t = 0;
-    bool cached = false;
-    {
-        std::lock_guard<std::mutex> lk(tune_mutex());
-        auto it = tune_cache().find(key);
-        if (it != tune_cache().end()) {
-            best = it->second.cfg;
-            best_c = it->second.cfg_c;
-            best_lanes = it->second.lanes;
-            cached = true;
-        }
-    }
-    if (!cached) {
+    TunePick pick;
+    const bool cached = cached_pick(key, &pick);
+    if (cached) {
+        best = pick.cfg;
+        best_c = pick.cfg_c;
+        best_lanes = pick.lanes;
+    } else {
         const bool prof = h->profiling;
         h->profiling = false;
         // coordinate search over group_max, warp_max, cta_max and the split
@@ -1846,8 +1863,11 @@ int cdmf_cuda_autotune(cdmf_handle* h, cdmf_bincfg* chosen, double* best_ms) {
         std::lock_guard<std::mutex> lk(tune_mutex());
         tune_cache()[key] = TunePick{best, best_c, best_lanes};
     }
-    h->group_lanes = best_lanes;
-    if ((r = replan(h, best, best_c))) return r;
+    // (a handle created with the cached pick already has these bins)
+    if (!(cached && best_lanes == h->group_lanes && same_cfg(best, h->cfg) && same_cfg(best_c, h->cfg_c))) {
+        h->group_lanes = best_lanes;
+        if ((r = replan(h, best, best_c))) return r;
+    }
     // the timing sweeps used the factors and residual as scratch
     if ((r = cdmf_cuda_set_factors(h, nullptr, nullptr))) return r;
     CU(h, cudaMemsetAsync(h->P, 0, sizeof(float2) * std::max<int64_t>(1, h->m), h->s));

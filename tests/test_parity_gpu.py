@@ -417,6 +417,25 @@ def test_autotune_leaves_unbinned_sweeps_alone(cpu_scale, opts):
         assert ms == 0 and cfg == before == e.bincfg()
 
 
+def test_autotune_pick_reused_by_next_handle(cpu_scale):
+    """A handle created with autotune on for a shape already tuned in this
+    process is planned with the kept pick from the start: same bins, and
+    results bit-identical to the handle before it."""
+    R, run, W0, ref = cpu_scale
+    outs = []
+    for _ in range(2):
+        with engine.Engine(R, run["k"], run["lambda_"], run["maxiter"], run["maxinneriter"], autotune=True,
+                           use_graph=True) as e:
+            cfg = e.bincfg()
+            e.set_factors(W0)
+            rm = e.run(run["maxiter"])
+            W, H = e.factors()
+            outs.append((cfg, W, H, rm))
+    (c0, W0_, H0_, r0), (c1, W1, H1, r1) = outs
+    assert c0 == c1
+    assert np.array_equal(bits(W0_), bits(W1)) and np.array_equal(bits(H0_), bits(H1)) and np.array_equal(r0, r1)
+
+
 def test_bincfg_change_after_graph_runs(cpu_scale):
     """A new bin plan after outer iterations were captured as CUDA graphs
     drops those graphs: the next runs take the new plan, bit for bit as an
