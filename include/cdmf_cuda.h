@@ -125,7 +125,8 @@ typedef struct {
 
 typedef struct cdmf_handle cdmf_handle;
 
-/* Called after every outer iteration: the reference's log-line values. */
+/* Called after every outer iteration: the reference's log-line values.
+ * train_ms_so_far: device time since the first outer iteration started. */
 typedef void (*cdmf_outer_cb)(int oiter, double rmse, double train_ms_so_far, void* user);
 
 /* The reference's defaults (src/pmf.h:4-26: k 10, lambda 0.1, 5 x 5
@@ -137,8 +138,11 @@ int cdmf_cuda_version(void);
 /* One call = the reference engine call (cdmf_ocl_01 / cdmf_ocl_02 / cdmf_csr5,
  * src/cdmf.h:6-10, called at src/main.cpp:43,50,57): upload, H := 0
  * (src/cdmf_ocl_1.cpp:64-68), maxiter outer iterations from the given W,
- * download W and H.
- * rmse_out (nullable) receives maxiter values when opts->rmse_each_outer. */
+ * download W and H.  Each outer iteration is queued before the previous
+ * one's RMSE is read back, so cb runs while the GPU works on the next one.
+ * rmse_out (nullable) receives maxiter values when opts->rmse_each_outer.
+ * A non-finite residual met by a refresh ends the call with
+ * CDMF_ERR_NUMERIC; W and H are then left as they were. */
 int cdmf_cuda_train(const cdmf_problem* p, const cdmf_opts* o, float* W, float* H,
                     double* rmse_out, cdmf_outer_cb cb, void* user);
 
