@@ -82,3 +82,22 @@ def test_reference_arm_contract_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_e2e_phase_times_are_captured():
+    """The e2e leg records the engine's phase times per call: the lines the
+    engine prints on stderr (fd 2) with verbose options are captured around
+    the call and parsed, and stderr is restored afterwards."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    def fake_call():
+        os.write(2, b"[cdmf] create: checks            3.7 ms\n[cdmf] create: relabel (GPU)     21.4 ms\n"
+                    b"[cdmf] train: create           31.4 ms\n[cdmf] train: outer loop      578.3 ms\n"
+                    b"unrelated line\n")
+        return 7
+
+    out, phases = bench.with_phase_times(fake_call)
+    assert out == 7
+    assert phases == {"create/checks": 3.7, "create/relabel (GPU)": 21.4, "create": 31.4, "outer loop": 578.3}
+    os.write(2, b"")   # fd 2 is usable again
